@@ -1,0 +1,522 @@
+// eval.cu -- strided gather/scatter and fused elementwise kernels.
+//
+// One kernel family serves copies (the empty program), fills (no inputs),
+// single infix operators and whole fused chains.  Two launch shapes:
+//
+//  ROW  -- the output and every input share the innermost canonical axis.
+//          Each thread handles VEC consecutive elements of one row; operands
+//          with unit (or reversed unit) inner stride use 128-bit accesses.
+//  TILE -- the output is contiguous along axis W while (some) inputs are
+//          contiguous along another axis R (permuted views).  A 64x64 tile of
+//          each such input is read coalesced along R into shared memory, then
+//          read back transposed so the output is written coalesced along W.
+#include "plan.h"
+#include "program.cuh"
+
+namespace phcu {
+
+struct EvalArgs {
+  EvalPlan plan;
+  phcu_program_t prog;
+  uint32_t* status;
+};
+
+constexpr int ROW_THREADS = 256;
+constexpr int TILE_THREADS = 256;
+
+// ------------------------------------------------------------------ ROW
+template <int NIN, int VEC>
+__global__ void __launch_bounds__(ROW_THREADS) eval_row_kernel(const __grid_constant__ EvalArgs A) {
+  const EvalPlan& p = A.plan;
+  const int rank = p.sp.rank;
+  const int W = rank - 1;
+  const uint32_t nchunks = (uint32_t)(p.sp.n / VEC);
+  uint32_t st = 0;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += gridDim.x * blockDim.x) {
+    const uint32_t e0 = c * VEC;
+    uint32_t row, col;
+    p.lendiv.divmod(e0, row, col);
+    int64_t off_out = (int64_t)col * p.out.stride[W];
+    int64_t off_in[NIN > 0 ? NIN : 1];
+#pragma unroll
+    for (int k = 0; k < NIN; k++) off_in[k] = (int64_t)col * p.in[k].stride[W];
+    // decompose the row index over the outer axes (innermost first)
+    uint32_t r = row;
+    for (int a = W - 1; a >= 0; a--) {
+      uint32_t q, x;
+      p.sp.div[a].divmod(r, q, x);
+      r = q;
+      off_out += (int64_t)x * p.out.stride[a];
+#pragma unroll
+      for (int k = 0; k < NIN; k++) off_in[k] += (int64_t)x * p.in[k].stride[a];
+    }
+    uint64_t in[NIN > 0 ? NIN : 1][VEC];
+#pragma unroll
+    for (int k = 0; k < NIN; k++) {
+      const int es = dtype_size(p.in[k].dtype);
+      load_operand<VEC>(p.in[k].base + off_in[k] * es, p.in[k].stride[W], p.in[k].dtype, p.in[k].vmode, in[k]);
+    }
+    uint64_t acc[VEC];
+    run_program<NIN, VEC>(A.prog, in, acc, st);
+    const int oes = dtype_size(p.out.dtype);
+    char* op = (char*)p.out.base + off_out * oes;
+    if (p.out.vmode == VM_VEC) {
+      store_vec<VEC>(op, p.out.dtype, acc);
+    } else {
+      store_scalar<VEC>(op, p.out.stride[W] * oes, p.out.dtype, acc);
+    }
+  }
+  if (st) report_status(A.status, st);
+}
+
+// ----------------------------------------------------------------- TILE
+// Shared memory: one TILE x (TILE+1) slot array per staged input, 8-byte slots.
+template <int NIN>
+__global__ void __launch_bounds__(TILE_THREADS) eval_tile_kernel(const __grid_constant__ EvalArgs A) {
+  extern __shared__ uint64_t smem[];
+  const EvalPlan& p = A.plan;
+  const int rank = p.sp.rank;
+  const int W = rank - 1;
+  const int R = p.raxis;
+  constexpr int LD = TILE + 1;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  constexpr int NWARP = TILE_THREADS / 32;
+  uint32_t st = 0;
+
+  const uint64_t ntiles = (uint64_t)p.tiles_w * p.tiles_r * p.nbatch;
+  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    uint32_t rest, tw, tr, b;
+    p.tdiv_w.divmod((uint32_t)t, rest, tw);
+    p.tdiv_r.divmod(rest, b, tr);
+    // batch coordinates (all axes except R and W)
+    int64_t off_out = 0;
+    int64_t off_in[NIN > 0 ? NIN : 1];
+#pragma unroll
+    for (int k = 0; k < NIN; k++) off_in[k] = 0;
+    uint32_t bb = b;
+    for (int a = W - 1; a >= 0; a--) {
+      if (a == R) continue;
+      uint32_t q, x;
+      p.sp.div[a].divmod(bb, q, x);
+      bb = q;
+      off_out += (int64_t)x * p.out.stride[a];
+#pragma unroll
+      for (int k = 0; k < NIN; k++) off_in[k] += (int64_t)x * p.in[k].stride[a];
+    }
+    const int64_t r0 = (int64_t)tr * TILE, w0 = (int64_t)tw * TILE;
+    const int64_t nr = min((int64_t)TILE, p.sp.shape[R] - r0);
+    const int64_t nw = min((int64_t)TILE, p.sp.shape[W] - w0);
+
+    // phase 1: staged inputs, coalesced along R
+    int slot = 0;
+#pragma unroll
+    for (int k = 0; k < NIN; k++) {
+      if (!(p.staged & (1u << k))) continue;
+      uint64_t* tile = smem + (size_t)slot * TILE * LD;
+      slot++;
+      const int es = dtype_size(p.in[k].dtype);
+      const char* base = p.in[k].base + (off_in[k] + r0 * p.in[k].stride[R] + w0 * p.in[k].stride[W]) * es;
+#pragma unroll
+      for (int i = 0; i < TILE / NWARP; i++) {
+        const int w = warp + i * NWARP;
+#pragma unroll
+        for (int j = 0; j < TILE / 32; j++) {
+          const int r = lane + 32 * j;
+          if (w < nw && r < nr) {
+            uint64_t v[1];
+            load_scalar<1>(base + ((int64_t)r * p.in[k].stride[R] + (int64_t)w * p.in[k].stride[W]) * es, 0,
+                           p.in[k].dtype, v);
+            tile[w * LD + r] = v[0];
+          }
+        }
+      }
+    }
+    if (p.staged) __syncthreads();
+
+    // phase 2: compute and write coalesced along W
+    const int oes = dtype_size(p.out.dtype);
+    char* obase = (char*)p.out.base + (off_out + r0 * p.out.stride[R] + w0) * oes;
+#pragma unroll 4
+    for (int i = 0; i < TILE / NWARP; i++) {
+      const int r = warp + i * NWARP;
+#pragma unroll
+      for (int j = 0; j < TILE / 32; j++) {
+        const int w = lane + 32 * j;
+        if (r < nr && w < nw) {
+          uint64_t in[NIN > 0 ? NIN : 1][1];
+          int s2 = 0;
+#pragma unroll
+          for (int k = 0; k < NIN; k++) {
+            if (p.staged & (1u << k)) {
+              in[k][0] = smem[(size_t)s2 * TILE * LD + w * LD + r];
+              s2++;
+            } else {
+              const int es = dtype_size(p.in[k].dtype);
+              uint64_t v[1];
+              load_scalar<1>(p.in[k].base + (off_in[k] + (r0 + r) * p.in[k].stride[R] +
+                                             (w0 + w) * p.in[k].stride[W]) * es,
+                             0, p.in[k].dtype, v);
+              in[k][0] = v[0];
+            }
+          }
+          uint64_t acc[1];
+          run_program<NIN, 1>(A.prog, in, acc, st);
+          uint64_t o[1] = {acc[0]};
+          store_scalar<1>(obase + ((int64_t)r * p.out.stride[R] + w) * oes, 0, p.out.dtype, o);
+        }
+      }
+    }
+    if (p.staged) __syncthreads();
+  }
+  if (st) report_status(A.status, st);
+}
+
+// ----------------------------------------------------------- dispatch
+template <int NIN>
+static int32_t launch_nin(const EvalArgs& A) {
+  const EvalPlan& p = A.plan;
+  Context& c = ctx();
+  if (p.mode == MODE_TILE) {
+    int nstaged = __builtin_popcount(p.staged);
+    size_t smem = (size_t)nstaged * TILE * (TILE + 1) * sizeof(uint64_t);
+    if (smem > 48 * 1024) {
+      cudaFuncSetAttribute(eval_tile_kernel<NIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    uint64_t ntiles = (uint64_t)p.tiles_w * p.tiles_r * p.nbatch;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_tile_kernel<NIN>, TILE_THREADS, smem);
+    if (per_sm < 1) per_sm = 1;
+    uint64_t grid = (uint64_t)c.sm_count * per_sm;
+    if (grid > ntiles) grid = ntiles;
+    eval_tile_kernel<NIN><<<(unsigned)grid, TILE_THREADS, smem, c.stream>>>(A);
+    count_launch();
+    return check_launch("eval_tile_kernel");
+  }
+  // ROW
+  uint64_t nchunks = (uint64_t)p.sp.n / p.vec;
+  uint64_t blocks = (nchunks + ROW_THREADS - 1) / ROW_THREADS;
+  uint64_t cap = (uint64_t)c.sm_count * (2048 / ROW_THREADS) * 4;
+  if (blocks > cap) blocks = cap;
+  if (blocks == 0) blocks = 1;
+  switch (p.vec) {
+    case 4: eval_row_kernel<NIN, 4><<<(unsigned)blocks, ROW_THREADS, 0, c.stream>>>(A); break;
+    case 2: eval_row_kernel<NIN, 2><<<(unsigned)blocks, ROW_THREADS, 0, c.stream>>>(A); break;
+    default: eval_row_kernel<NIN, 1><<<(unsigned)blocks, ROW_THREADS, 0, c.stream>>>(A); break;
+  }
+  count_launch();
+  return check_launch("eval_row_kernel");
+}
+
+int32_t launch_eval(const EvalArgs& A) {
+  switch (A.plan.nin) {
+    case 0: return launch_nin<0>(A);
+    case 1: return launch_nin<1>(A);
+    case 2: return launch_nin<2>(A);
+    case 3: return launch_nin<3>(A);
+    case 4: return launch_nin<4>(A);
+  }
+  return fail(PHCU_ERR_INVALID, "too many inputs (%d > %d)", A.plan.nin, MAXIN);
+}
+
+// ------------------------------------------------------- program checks
+static int32_t check_program(const phcu_program_t* prog, int nin) {
+  if (!prog) return fail(PHCU_ERR_INVALID, "null program");
+  if (prog->n_instr < 0 || prog->n_instr > PHCU_MAX_INSTR)
+    return fail(PHCU_ERR_INVALID, "program length %d outside 0..%d", prog->n_instr, PHCU_MAX_INSTR);
+  for (int i = 0; i < prog->n_instr; i++) {
+    const phcu_instr_t& I = prog->code[i];
+    if (!dtype_valid(I.type)) return fail(PHCU_ERR_INVALID, "instruction %d: bad type %d", i, I.type);
+    bool needs_b = !(I.op == PHCU_I_ST0 || I.op == PHCU_I_ST1 || I.op == PHCU_I_CVT || I.op == PHCU_I_NEG ||
+                     I.op == PHCU_I_NOT || I.op == PHCU_I_POS);
+    if (needs_b) {
+      if (!(I.src < nin || I.src == PHCU_SRC_IMM || I.src == PHCU_SRC_S0 || I.src == PHCU_SRC_S1))
+        return fail(PHCU_ERR_INVALID, "instruction %d: operand source %d not available", i, I.src);
+      if (!dtype_valid(I.btype)) return fail(PHCU_ERR_INVALID, "instruction %d: bad operand type", i);
+    }
+    if (!(I.op < PHCU_OP_NBINARY || (I.op >= PHCU_I_LD && I.op <= PHCU_I_POS)))
+      return fail(PHCU_ERR_INVALID, "instruction %d: unknown opcode %d", i, I.op);
+    if (I.op == PHCU_I_CVT && !dtype_valid((int)I.imm.i))
+      return fail(PHCU_ERR_INVALID, "instruction %d: bad conversion target", i);
+  }
+  return PHCU_OK;
+}
+
+// Evaluates with inputs that may overlap the output: an input that overlaps
+// the output with a different mapping is first copied to a temporary.
+int32_t eval_views(const phcu_program_t* prog, const phcu_view_t* inputs, int nin, const phcu_view_t* out,
+                   int force_mode = -1) {
+  PHCU_TRY(require_ctx());
+  PHCU_TRY(check_view(out, "output"));
+  if (nin < 0 || nin > MAXIN) return fail(PHCU_ERR_INVALID, "n_inputs %d outside 0..%d", nin, MAXIN);
+  for (int k = 0; k < nin; k++) PHCU_TRY(check_view(&inputs[k], "input"));
+  PHCU_TRY(check_program(prog, nin));
+  if (prog->out_type != out->dtype)
+    return fail(PHCU_ERR_INVALID, "program result type %d differs from output dtype %d", prog->out_type, out->dtype);
+
+  phcu_view_t staged[MAXIN];
+  void* temps[MAXIN] = {nullptr};
+  const phcu_view_t* ins[MAXIN];
+  for (int k = 0; k < nin; k++) {
+    ins[k] = &inputs[k];
+    if (views_overlap(&inputs[k], out) && !views_identical(&inputs[k], out)) {
+      // materialise this input first (lexicographic, contiguous)
+      const phcu_view_t& v = inputs[k];
+      int64_t n = view_size(&v);
+      PHCU_TRY(scratch_alloc((size_t)n * dtype_size(v.dtype), &temps[k]));
+      phcu_view_t t;
+      memset(&t, 0, sizeof(t));
+      t.base = temps[k];
+      t.dtype = v.dtype;
+      t.rank = v.rank;
+      int64_t s = 1;
+      for (int i = v.rank - 1; i >= 0; i--) {
+        t.shape[i] = v.shape[i];
+        t.stride[i] = s;
+        s *= v.shape[i];
+      }
+      EvalArgs C;
+      phcu_program_t cp;
+      memset(&cp, 0, sizeof(cp));
+      cp.n_instr = 1;
+      cp.out_type = v.dtype;
+      cp.code[0].op = PHCU_I_LD;
+      cp.code[0].src = 0;
+      cp.code[0].type = (uint8_t)v.dtype;
+      cp.code[0].btype = (uint8_t)v.dtype;
+      const phcu_view_t* one[1] = {&v};
+      PHCU_TRY(make_plan(&t, one, 1, &C.plan));
+      C.prog = cp;
+      C.status = ctx().status;
+      if (C.plan.mode != MODE_EMPTY) PHCU_TRY(launch_eval(C));
+      staged[k] = t;
+      ins[k] = &staged[k];
+    }
+  }
+  EvalArgs A;
+  int32_t rc = make_plan(out, ins, nin, &A.plan, force_mode);
+  if (rc == PHCU_OK && A.plan.mode != MODE_EMPTY) {
+    A.prog = *prog;
+    A.status = ctx().status;
+    rc = launch_eval(A);
+  }
+  for (int k = 0; k < nin; k++) scratch_free(temps[k]);
+  return rc;
+}
+
+// ------------------------------------------------ Crystal result types
+int32_t result_dtype(int op, int ta, int tb, int* tout) {
+  if (ta == PHCU_BOOL || tb == PHCU_BOOL) {
+    if (op == PHCU_OP_EQ) { *tout = PHCU_BOOL; return PHCU_OK; }
+    if (ta == PHCU_BOOL && tb == PHCU_BOOL && (op == PHCU_OP_AND || op == PHCU_OP_OR || op == PHCU_OP_XOR)) {
+      *tout = PHCU_BOOL;
+      return PHCU_OK;
+    }
+    return fail(PHCU_ERR_UNSUPPORTED, "operator %d is not defined for Bool operands", op);
+  }
+  if (op == PHCU_OP_GT || op == PHCU_OP_LT || op == PHCU_OP_GE || op == PHCU_OP_LE || op == PHCU_OP_EQ) {
+    *tout = PHCU_BOOL;
+    return PHCU_OK;
+  }
+  if (op == PHCU_OP_CMP) { *tout = PHCU_I32; return PHCU_OK; }
+  if (op == PHCU_OP_AND || op == PHCU_OP_OR || op == PHCU_OP_XOR) {
+    if (!is_int_t(ta) || !is_int_t(tb)) return fail(PHCU_ERR_UNSUPPORTED, "bitwise operator on a float operand");
+    *tout = ta;
+    return PHCU_OK;
+  }
+  if (is_int_t(ta) && is_int_t(tb)) {
+    *tout = (op == PHCU_OP_DIV) ? PHCU_F64 : ta;
+    return PHCU_OK;
+  }
+  if (op == PHCU_OP_WADD || op == PHCU_OP_WSUB || op == PHCU_OP_WMUL || op == PHCU_OP_WPOW)
+    return fail(PHCU_ERR_UNSUPPORTED, "wrapping operator on a float operand");
+  if (is_int_t(ta) && is_float_t(tb) && op == PHCU_OP_POW) { *tout = PHCU_F64; return PHCU_OK; }
+  *tout = (ta == PHCU_F64 || tb == PHCU_F64) ? PHCU_F64 : PHCU_F32;
+  return PHCU_OK;
+}
+
+// compute type of `a op b` before the result conversion
+static int compute_type(int op, int ta, int tb) {
+  if (ta == PHCU_BOOL && tb == PHCU_BOOL) return PHCU_BOOL;
+  if (is_int_t(ta) && is_int_t(tb)) return ta;
+  if (is_int_t(ta) && is_float_t(tb) && op == PHCU_OP_POW) return PHCU_F64;
+  return (ta == PHCU_F64 || tb == PHCU_F64) ? PHCU_F64 : PHCU_F32;
+}
+
+// Builds the one-operator program ACC = IN0 op B.
+static int32_t binary_program(int op, int ta, int tb, int src_b, const phcu_scalar_t* imm, int scalar_left,
+                              phcu_program_t* P) {
+  int tout;
+  PHCU_TRY(result_dtype(op, ta, tb, &tout));
+  memset(P, 0, sizeof(*P));
+  if (ta == PHCU_BOOL || tb == PHCU_BOOL) {
+    if (!(ta == PHCU_BOOL && tb == PHCU_BOOL)) {
+      // Bool == number is always false (different types)
+      P->n_instr = 1;
+      P->code[0].op = PHCU_I_LD;
+      P->code[0].src = PHCU_SRC_IMM;
+      P->code[0].type = PHCU_BOOL;
+      P->code[0].btype = PHCU_BOOL;
+      P->code[0].imm.i = 0;
+      P->out_type = PHCU_BOOL;
+      return PHCU_OK;
+    }
+  }
+  int T = compute_type(op, ta, tb);
+  if (op == PHCU_OP_POW && is_float_t(ta) && is_int_t(tb)) T = ta;  // powi keeps the base type
+  int n = 0;
+  // ACC = IN0 (converted to T unless it is an integer exponent of a float base)
+  auto slot_of = [](const phcu_scalar_t* s) -> int64_t {
+    switch (s->dtype) {
+      case PHCU_F32: { float f = (float)s->v.f; uint32_t u; memcpy(&u, &f, 4); return (int64_t)u; }
+      case PHCU_F64: { int64_t u; memcpy(&u, &s->v.f, 8); return u; }
+      case PHCU_I32: return (int64_t)(uint32_t)(int32_t)s->v.i;
+      case PHCU_BOOL: return s->v.i ? 1 : 0;
+      default: return s->v.i;
+    }
+  };
+  if (scalar_left) {
+    // scalar op IN0: ACC = scalar, B = IN0
+    if (op == PHCU_OP_POW && is_float_t(ta) && is_int_t(tb)) {
+      // float scalar ** int array: powi(scalar, x)
+      phcu_instr_t& a = P->code[n++];
+      a.op = PHCU_I_LD; a.src = 0; a.type = (uint8_t)tb; a.btype = (uint8_t)tb;
+      phcu_instr_t& s0 = P->code[n++];
+      s0.op = PHCU_I_ST0; s0.type = (uint8_t)tb;
+      phcu_instr_t& l = P->code[n++];
+      l.op = PHCU_I_LD; l.src = PHCU_SRC_IMM; l.type = (uint8_t)T; l.btype = (uint8_t)ta; l.imm.i = slot_of(imm);
+      phcu_instr_t& pw = P->code[n++];
+      pw.op = PHCU_OP_POW; pw.src = PHCU_SRC_S0; pw.type = (uint8_t)T; pw.btype = (uint8_t)tb;
+    } else {
+      phcu_instr_t& l = P->code[n++];
+      l.op = PHCU_I_LD; l.src = PHCU_SRC_IMM; l.type = (uint8_t)T; l.btype = (uint8_t)ta; l.imm.i = slot_of(imm);
+      phcu_instr_t& o = P->code[n++];
+      o.op = (uint8_t)op; o.src = 0; o.type = (uint8_t)T; o.btype = (uint8_t)tb;
+    }
+  } else {
+    phcu_instr_t& l = P->code[n++];
+    l.op = PHCU_I_LD; l.src = 0; l.type = (uint8_t)T; l.btype = (uint8_t)ta;
+    phcu_instr_t& o = P->code[n++];
+    o.op = (uint8_t)op;
+    o.src = (uint8_t)src_b;
+    o.type = (uint8_t)T;
+    o.btype = (uint8_t)tb;
+    if (src_b == PHCU_SRC_IMM) o.imm.i = slot_of(imm);
+  }
+  // result type of the operator in T
+  int rt = T;
+  if (op == PHCU_OP_GT || op == PHCU_OP_LT || op == PHCU_OP_GE || op == PHCU_OP_LE || op == PHCU_OP_EQ) rt = PHCU_BOOL;
+  else if (op == PHCU_OP_CMP) rt = PHCU_I32;
+  else if (op == PHCU_OP_DIV && is_int_t(T)) rt = PHCU_F64;
+  if (rt != tout) {
+    phcu_instr_t& c = P->code[n++];
+    c.op = PHCU_I_CVT; c.type = (uint8_t)rt; c.imm.i = tout;
+  }
+  P->n_instr = n;
+  P->out_type = tout;
+  return PHCU_OK;
+}
+
+}  // namespace phcu
+
+using namespace phcu;
+
+extern "C" {
+
+int32_t phcu_result_dtype(int32_t op, int32_t ta, int32_t tb, int32_t* tout) {
+  int t;
+  PHCU_TRY(result_dtype(op, ta, tb, &t));
+  *tout = t;
+  return PHCU_OK;
+}
+
+int32_t phcu_copy(const phcu_view_t* dst, const phcu_view_t* src) {
+  PHCU_TRY(require_ctx());
+  PHCU_TRY(check_view(dst, "dst"));
+  PHCU_TRY(check_view(src, "src"));
+  if (dst->dtype != src->dtype)
+    return fail(PHCU_ERR_INVALID, "phcu_copy: dtype %d -> %d (copies do not convert)", src->dtype, dst->dtype);
+  if (view_size(dst) != view_size(src))
+    return fail(PHCU_ERR_SHAPE, "phcu_copy: source has %lld elements, destination %lld", (long long)view_size(src),
+                (long long)view_size(dst));
+  phcu_program_t P;
+  memset(&P, 0, sizeof(P));
+  P.n_instr = 1;
+  P.out_type = dst->dtype;
+  P.code[0].op = PHCU_I_LD;
+  P.code[0].src = 0;
+  P.code[0].type = (uint8_t)dst->dtype;
+  P.code[0].btype = (uint8_t)dst->dtype;
+  return eval_views(&P, src, 1, dst);
+}
+
+int32_t phcu_fill(const phcu_view_t* dst, const phcu_scalar_t* value) {
+  PHCU_TRY(require_ctx());
+  PHCU_TRY(check_view(dst, "dst"));
+  if (!value) return fail(PHCU_ERR_INVALID, "phcu_fill: null value");
+  phcu_program_t P;
+  memset(&P, 0, sizeof(P));
+  P.n_instr = 1;
+  P.out_type = dst->dtype;
+  phcu_instr_t& I = P.code[0];
+  I.op = PHCU_I_LD;
+  I.src = PHCU_SRC_IMM;
+  I.type = (uint8_t)dst->dtype;
+  I.btype = (uint8_t)value->dtype;
+  switch (value->dtype) {
+    case PHCU_F32: { float f = (float)value->v.f; uint32_t u; memcpy(&u, &f, 4); I.imm.i = u; break; }
+    case PHCU_F64: memcpy(&I.imm.i, &value->v.f, 8); break;
+    case PHCU_I32: I.imm.i = (int64_t)(uint32_t)(int32_t)value->v.i; break;
+    case PHCU_BOOL: I.imm.i = value->v.i ? 1 : 0; break;
+    default: I.imm.i = value->v.i;
+  }
+  return eval_views(&P, nullptr, 0, dst);
+}
+
+int32_t phcu_eval(const phcu_program_t* prog, const phcu_view_t* inputs, int32_t n_inputs, const phcu_view_t* out) {
+  return eval_views(prog, inputs, n_inputs, out);
+}
+
+int32_t phcu_binary(int32_t op, const phcu_view_t* a, const phcu_view_t* b, const phcu_view_t* out) {
+  PHCU_TRY(require_ctx());
+  PHCU_TRY(check_view(a, "a"));
+  PHCU_TRY(check_view(b, "b"));
+  if (op < 0 || op >= PHCU_OP_NBINARY) return fail(PHCU_ERR_INVALID, "unknown operator %d", op);
+  phcu_program_t P;
+  PHCU_TRY(binary_program(op, a->dtype, b->dtype, 1, nullptr, 0, &P));
+  phcu_view_t ins[2] = {*a, *b};
+  return eval_views(&P, ins, 2, out);
+}
+
+int32_t phcu_binary_scalar(int32_t op, const phcu_view_t* a, const phcu_scalar_t* s, int32_t scalar_left,
+                           const phcu_view_t* out) {
+  PHCU_TRY(require_ctx());
+  PHCU_TRY(check_view(a, "a"));
+  if (!s || !dtype_valid(s->dtype)) return fail(PHCU_ERR_INVALID, "bad scalar");
+  if (op < 0 || op >= PHCU_OP_NBINARY) return fail(PHCU_ERR_INVALID, "unknown operator %d", op);
+  phcu_program_t P;
+  if (scalar_left) PHCU_TRY(binary_program(op, s->dtype, a->dtype, PHCU_SRC_IMM, s, 1, &P));
+  else PHCU_TRY(binary_program(op, a->dtype, s->dtype, PHCU_SRC_IMM, s, 0, &P));
+  return eval_views(&P, a, 1, out);
+}
+
+int32_t phcu_unary(int32_t uop, const phcu_view_t* a, const phcu_view_t* out) {
+  PHCU_TRY(require_ctx());
+  PHCU_TRY(check_view(a, "a"));
+  int t = a->dtype;
+  if (t == PHCU_BOOL) return fail(PHCU_ERR_UNSUPPORTED, "unary operator on Bool");
+  if (uop == PHCU_UOP_NOT && !is_int_t(t)) return fail(PHCU_ERR_UNSUPPORTED, "~ on a float operand");
+  phcu_program_t P;
+  memset(&P, 0, sizeof(P));
+  P.n_instr = 2;
+  P.out_type = t;
+  P.code[0].op = PHCU_I_LD;
+  P.code[0].src = 0;
+  P.code[0].type = (uint8_t)t;
+  P.code[0].btype = (uint8_t)t;
+  P.code[1].op = uop == PHCU_UOP_NEG ? PHCU_I_NEG : uop == PHCU_UOP_NOT ? PHCU_I_NOT : PHCU_I_POS;
+  P.code[1].type = (uint8_t)t;
+  return eval_views(&P, a, 1, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,278 @@
+// runtime.cu -- context, memory, status word, timers, graphs and errors.
+#include <stdarg.h>
+#include <stdio.h>
+
+#include "common.cuh"
+
+namespace phcu {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int32_t fail(int32_t code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int32_t cuda_fail(cudaError_t e, const char* what) {
+  snprintf(g_err, sizeof(g_err), "CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+  if (e == cudaErrorMemoryAllocation) return PHCU_ERR_OOM;
+  return PHCU_ERR_CUDA;
+}
+
+static Context g_ctx;
+Context& ctx() { return g_ctx; }
+
+int32_t require_ctx() {
+  if (!g_ctx.ready) return fail(PHCU_ERR_NOT_INIT, "phcu_init has not been called");
+  return PHCU_OK;
+}
+
+int32_t check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return PHCU_OK;
+}
+
+int32_t scratch_alloc(size_t bytes, void** p) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMallocAsync(p, bytes, g_ctx.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(scratch)");
+  return PHCU_OK;
+}
+
+void scratch_free(void* p) {
+  if (p) cudaFreeAsync(p, g_ctx.stream);
+}
+
+struct Timer {
+  cudaEvent_t a, b;
+};
+
+}  // namespace phcu
+
+using namespace phcu;
+
+extern "C" {
+
+int32_t phcu_init(int32_t device) {
+  Context& c = g_ctx;
+  if (c.ready && c.device == device) return PHCU_OK;
+  if (c.ready) return fail(PHCU_ERR_INVALID, "phcu_init: already initialised on device %d", c.device);
+  PHCU_CUDA(cudaSetDevice(device));
+  PHCU_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking));
+  c.stream = c.own_stream;
+  PHCU_CUDA(cudaMalloc(&c.status, sizeof(uint32_t)));
+  PHCU_CUDA(cudaMemset(c.status, 0, sizeof(uint32_t)));
+  cudaDeviceProp prop;
+  PHCU_CUDA(cudaGetDeviceProperties(&prop, device));
+  c.sm_count = prop.multiProcessorCount;
+  c.l2_bytes = prop.l2CacheSize;
+  c.smem_optin = (int)prop.sharedMemPerBlockOptin;
+  int clk = 0;
+  cudaDeviceGetAttribute(&clk, cudaDevAttrClockRate, device);
+  c.clock_khz = clk;
+  // keep freed scratch in the pool instead of returning it to the driver
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  c.device = device;
+  c.launches = 0;
+  c.ready = true;
+  return PHCU_OK;
+}
+
+int32_t phcu_shutdown(void) {
+  Context& c = g_ctx;
+  if (!c.ready) return PHCU_OK;
+  cudaStreamSynchronize(c.stream);
+  if (c.l2_scrub) cudaFree(c.l2_scrub);
+  cudaFree(c.status);
+  cudaStreamDestroy(c.own_stream);
+  c = Context();
+  return PHCU_OK;
+}
+
+int32_t phcu_set_stream(void* s) {
+  PHCU_TRY(require_ctx());
+  g_ctx.stream = s ? (cudaStream_t)s : g_ctx.own_stream;
+  return PHCU_OK;
+}
+
+int32_t phcu_get_stream(void** s) {
+  PHCU_TRY(require_ctx());
+  *s = (void*)g_ctx.stream;
+  return PHCU_OK;
+}
+
+int32_t phcu_sync(void) {
+  PHCU_TRY(require_ctx());
+  PHCU_CUDA(cudaStreamSynchronize(g_ctx.stream));
+  return PHCU_OK;
+}
+
+int32_t phcu_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return PHCU_ERR_INVALID;
+  snprintf(buf, len, "%s", g_err);
+  return PHCU_OK;
+}
+
+int32_t phcu_status_word(uint32_t* out, int32_t clear) {
+  PHCU_TRY(require_ctx());
+  uint32_t v = 0;
+  PHCU_CUDA(cudaMemcpyAsync(&v, g_ctx.status, sizeof(v), cudaMemcpyDeviceToHost, g_ctx.stream));
+  PHCU_CUDA(cudaStreamSynchronize(g_ctx.stream));
+  if (clear && v) {
+    PHCU_CUDA(cudaMemsetAsync(g_ctx.status, 0, sizeof(uint32_t), g_ctx.stream));
+    PHCU_CUDA(cudaStreamSynchronize(g_ctx.stream));
+  }
+  *out = v;
+  return PHCU_OK;
+}
+
+int32_t phcu_version(int32_t* major, int32_t* minor) {
+  *major = PHCU_VERSION_MAJOR;
+  *minor = PHCU_VERSION_MINOR;
+  return PHCU_OK;
+}
+
+int32_t phcu_device_info(int32_t* sm_count, int64_t* l2_bytes, int32_t* smem_per_block,
+                         int32_t* clock_khz) {
+  PHCU_TRY(require_ctx());
+  if (sm_count) *sm_count = g_ctx.sm_count;
+  if (l2_bytes) *l2_bytes = g_ctx.l2_bytes;
+  if (smem_per_block) *smem_per_block = g_ctx.smem_optin;
+  if (clock_khz) *clock_khz = g_ctx.clock_khz;
+  return PHCU_OK;
+}
+
+int32_t phcu_alloc(size_t bytes, void** dptr) {
+  PHCU_TRY(require_ctx());
+  if (!dptr) return fail(PHCU_ERR_INVALID, "phcu_alloc: null output pointer");
+  if (bytes == 0) bytes = 16;  // keep every array addressable
+  cudaError_t e = cudaMallocAsync(dptr, bytes, g_ctx.stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync");
+  return PHCU_OK;
+}
+
+int32_t phcu_free(void* dptr) {
+  PHCU_TRY(require_ctx());
+  if (!dptr) return PHCU_OK;
+  PHCU_CUDA(cudaFreeAsync(dptr, g_ctx.stream));
+  return PHCU_OK;
+}
+
+int32_t phcu_host_alloc(size_t bytes, void** hptr) {
+  PHCU_TRY(require_ctx());
+  PHCU_CUDA(cudaMallocHost(hptr, bytes ? bytes : 16));
+  return PHCU_OK;
+}
+
+int32_t phcu_host_free(void* hptr) {
+  if (hptr) PHCU_CUDA(cudaFreeHost(hptr));
+  return PHCU_OK;
+}
+
+int32_t phcu_upload(void* dst, const void* src, size_t bytes) {
+  PHCU_TRY(require_ctx());
+  if (bytes == 0) return PHCU_OK;
+  PHCU_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g_ctx.stream));
+  return PHCU_OK;
+}
+
+int32_t phcu_download(void* dst, const void* src, size_t bytes) {
+  PHCU_TRY(require_ctx());
+  if (bytes == 0) return PHCU_OK;
+  PHCU_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g_ctx.stream));
+  PHCU_CUDA(cudaStreamSynchronize(g_ctx.stream));
+  return PHCU_OK;
+}
+
+int32_t phcu_memset(void* dptr, int32_t value, size_t bytes) {
+  PHCU_TRY(require_ctx());
+  if (bytes == 0) return PHCU_OK;
+  PHCU_CUDA(cudaMemsetAsync(dptr, value, bytes, g_ctx.stream));
+  return PHCU_OK;
+}
+
+int32_t phcu_graph_begin(void) {
+  PHCU_TRY(require_ctx());
+  if (g_ctx.stream == 0) return fail(PHCU_ERR_INVALID, "cannot capture the legacy default stream");
+  PHCU_CUDA(cudaStreamBeginCapture(g_ctx.stream, cudaStreamCaptureModeThreadLocal));
+  return PHCU_OK;
+}
+
+int32_t phcu_graph_end(void** graph_exec) {
+  PHCU_TRY(require_ctx());
+  cudaGraph_t g;
+  PHCU_CUDA(cudaStreamEndCapture(g_ctx.stream, &g));
+  cudaGraphExec_t ge;
+  cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  *graph_exec = (void*)ge;
+  return PHCU_OK;
+}
+
+int32_t phcu_graph_launch(void* graph_exec) {
+  PHCU_TRY(require_ctx());
+  PHCU_CUDA(cudaGraphLaunch((cudaGraphExec_t)graph_exec, g_ctx.stream));
+  return PHCU_OK;
+}
+
+int32_t phcu_graph_destroy(void* graph_exec) {
+  if (graph_exec) PHCU_CUDA(cudaGraphExecDestroy((cudaGraphExec_t)graph_exec));
+  return PHCU_OK;
+}
+
+int32_t phcu_timer_start(void** timer) {
+  PHCU_TRY(require_ctx());
+  Timer* t = new Timer();
+  PHCU_CUDA(cudaEventCreate(&t->a));
+  PHCU_CUDA(cudaEventCreate(&t->b));
+  PHCU_CUDA(cudaEventRecord(t->a, g_ctx.stream));
+  *timer = t;
+  return PHCU_OK;
+}
+
+int32_t phcu_timer_stop(void* timer, float* ms) {
+  PHCU_TRY(require_ctx());
+  Timer* t = (Timer*)timer;
+  PHCU_CUDA(cudaEventRecord(t->b, g_ctx.stream));
+  PHCU_CUDA(cudaEventSynchronize(t->b));
+  PHCU_CUDA(cudaEventElapsedTime(ms, t->a, t->b));
+  cudaEventDestroy(t->a);
+  cudaEventDestroy(t->b);
+  delete t;
+  return PHCU_OK;
+}
+
+int32_t phcu_launch_count(uint64_t* n) {
+  *n = g_ctx.launches;
+  return PHCU_OK;
+}
+
+int32_t phcu_l2_flush(void) {
+  PHCU_TRY(require_ctx());
+  Context& c = g_ctx;
+  size_t want = (size_t)(c.l2_bytes > 0 ? c.l2_bytes : (128ll << 20)) * 2;
+  if (!c.l2_scrub) {
+    PHCU_CUDA(cudaMalloc(&c.l2_scrub, want));
+    c.l2_scrub_bytes = want;
+  }
+  PHCU_CUDA(cudaMemsetAsync(c.l2_scrub, c.launches & 0xff, c.l2_scrub_bytes, c.stream));
+  return PHCU_OK;
+}
+
+}  // extern "C"

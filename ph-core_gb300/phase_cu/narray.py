@@ -1,0 +1,1262 @@
+"""Phase::CuNArray and its views: the MultiIndexable/MultiWritable surface on
+device memory.
+
+Mirrors the reference operator API (src/multi_indexable.cr, src/multi_writable.cr,
+src/n_array.cr, src/view.cr, src/proc_view.cr, src/mutable_view.cr): same
+method names (snake_case), argument meaning and exceptions.  Every bulk
+method runs one library call; nothing is evaluated element by element on the
+host.  Region validation happens here (as in the reference); the library
+receives affine view descriptors.
+
+  CuNArray       -- owns a contiguous row-major device buffer (NArray)
+  CuView         -- lazy aliasing view: base buffer + affine map (View)
+  CuMutableView  -- writable view (MutableView)
+  CuProcView     -- lazy elementwise program over views (ProcView); infix
+                    operators on it stay lazy and compile into ONE kernel
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import _abi as A
+from .errors import ArgumentError, DimensionError, EmptyError, ShapeError
+from .region import IndexRegion, check_region_fits, compatible_shapes, normalise_literal, shape_to_size
+
+# ----------------------------------------------------------------- context
+_ready = False
+
+
+class config:
+    """eager_errors: after an operation that can raise (checked integer
+    arithmetic, float modulo), wait for it and raise like the reference does.
+    When False, device errors surface at the next check_errors() call."""
+
+    eager_errors = True
+
+
+def init(device=None):
+    global _ready
+    if _ready:
+        return
+    lib = A.load()
+    dev = int(os.environ.get("PHCU_DEVICE", "0")) if device is None else int(device)
+    A.check(lib.phcu_init(dev), "phcu_init")
+    _ready = True
+
+
+def lib():
+    init()
+    return A.load()
+
+
+def sync():
+    A.call("phcu_sync") if _ready else None
+
+
+def check_errors():
+    """Reads and clears the device status word; raises the matching exception."""
+    init()
+    w = ctypes.c_uint32(0)
+    A.check(lib().phcu_status_word(ctypes.byref(w), 1), "phcu_status_word")
+    v = w.value
+    if v & A.ST_DIVZERO:
+        from .errors import DivisionByZeroError
+        raise DivisionByZeroError("Division by 0")
+    if v & A.ST_OVERFLOW:
+        raise OverflowError("Arithmetic overflow")
+    if v & A.ST_ARGUMENT:
+        raise ArgumentError("Cannot raise an integer to a negative integer power, use floats for that")
+    if v & A.ST_TIMEOUT:
+        from .errors import DeviceError
+        raise DeviceError("device work queue timed out")
+
+
+# ------------------------------------------------------------------ dtypes
+_NP = {A.BOOL: np.bool_, A.I32: np.int32, A.I64: np.int64, A.F32: np.float32, A.F64: np.float64}
+_FROM_NP = {np.dtype(np.bool_): A.BOOL, np.dtype(np.int32): A.I32, np.dtype(np.int64): A.I64,
+            np.dtype(np.float32): A.F32, np.dtype(np.float64): A.F64}
+
+Bool, Int32, Int64, Float32, Float64 = A.BOOL, A.I32, A.I64, A.F32, A.F64
+
+
+def dtype_of_numpy(dt):
+    dt = np.dtype(dt)
+    if dt not in _FROM_NP:
+        raise TypeError("unsupported element type %s" % dt)
+    return _FROM_NP[dt]
+
+
+def np_dtype(t):
+    return _NP[t]
+
+
+def _is_int(t):
+    return t in (A.I32, A.I64)
+
+
+def _is_float(t):
+    return t in (A.F32, A.F64)
+
+
+def scalar_dtype(v):
+    """Crystal literal type of a Python scalar: int -> Int32 (Int64 if it does
+    not fit), float -> Float64, bool -> Bool; numpy scalars keep their type."""
+    if isinstance(v, (bool, np.bool_)):
+        return A.BOOL
+    if isinstance(v, np.generic):
+        return dtype_of_numpy(v.dtype)
+    if isinstance(v, int):
+        return A.I32 if -2 ** 31 <= v < 2 ** 31 else A.I64
+    if isinstance(v, float):
+        return A.F64
+    raise TypeError("unsupported scalar %r" % (v,))
+
+
+def result_dtype(op, ta, tb):
+    """Crystal result type of `a op b` (same rules as the library)."""
+    if ta == A.BOOL or tb == A.BOOL:
+        if op == A.OP_EQ:
+            return A.BOOL
+        if ta == A.BOOL and tb == A.BOOL and op in (A.OP_AND, A.OP_OR, A.OP_XOR):
+            return A.BOOL
+        raise NotImplementedError("operator is not defined for Bool operands")
+    if op in (A.OP_GT, A.OP_LT, A.OP_GE, A.OP_LE, A.OP_EQ):
+        return A.BOOL
+    if op == A.OP_CMP:
+        return A.I32
+    if op in (A.OP_AND, A.OP_OR, A.OP_XOR):
+        if not (_is_int(ta) and _is_int(tb)):
+            raise NotImplementedError("bitwise operator on a float operand")
+        return ta
+    if _is_int(ta) and _is_int(tb):
+        return A.F64 if op == A.OP_DIV else ta
+    if op in (A.OP_WADD, A.OP_WSUB, A.OP_WMUL, A.OP_WPOW):
+        raise NotImplementedError("wrapping operator on a float operand")
+    if _is_int(ta) and _is_float(tb) and op == A.OP_POW:
+        return A.F64
+    return A.F64 if A.F64 in (ta, tb) else A.F32
+
+
+def _compute_type(op, ta, tb):
+    if ta == A.BOOL and tb == A.BOOL:
+        return A.BOOL
+    if _is_int(ta) and _is_int(tb):
+        return ta
+    if op == A.OP_POW and _is_float(ta) and _is_int(tb):
+        return ta
+    if _is_int(ta) and _is_float(tb) and op == A.OP_POW:
+        return A.F64
+    return A.F64 if A.F64 in (ta, tb) else A.F32
+
+
+def _slot_bits(value, t):
+    """Bit pattern of a value in a 64-bit program slot of type t."""
+    if t == A.F32:
+        return int(np.array(value, dtype=np.float32).view(np.uint32))
+    if t == A.F64:
+        return int(np.array(value, dtype=np.float64).view(np.int64))
+    if t == A.I32:
+        return int(np.array(int(value), dtype=np.int64).astype(np.int32).view(np.uint32))
+    if t == A.BOOL:
+        return 1 if value else 0
+    return int(np.int64(int(value)))
+
+
+def _cast_scalar(value, t):
+    return np.array(value).astype(_NP[t])[()]
+
+
+# --------------------------------------------------------------- buffers
+class _Buffer:
+    """Device allocation owned by a CuNArray (freed when the last user goes)."""
+
+    __slots__ = ("ptr", "nbytes", "__weakref__")
+
+    def __init__(self, nbytes):
+        init()
+        p = ctypes.c_void_p()
+        A.check(lib().phcu_alloc(max(int(nbytes), 1), ctypes.byref(p)), "phcu_alloc")
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+
+    def __del__(self):
+        try:
+            if self.ptr and A._lib is not None:
+                A._lib.phcu_free(self.ptr)
+        except Exception:
+            pass
+        self.ptr = None
+
+
+def _row_major(shape):
+    st = [0] * len(shape)
+    s = 1
+    for i in range(len(shape) - 1, -1, -1):
+        st[i] = s
+        s *= shape[i]
+    return st
+
+
+def _make_view(buf, dtype, offset, shape, stride):
+    v = A.View()
+    v.base = buf.ptr if buf is not None else None
+    v.dtype = dtype
+    v.rank = len(shape)
+    v.offset = offset
+    if len(shape) > A.MAX_RANK:
+        raise DimensionError("rank %d exceeds the device limit of %d" % (len(shape), A.MAX_RANK))
+    for i, (n, s) in enumerate(zip(shape, stride)):
+        v.shape[i] = n
+        v.stride[i] = s
+    return v
+
+
+# ------------------------------------------------- affine transform algebra
+def _affine_region(offset, shape, stride, region):
+    """Folds a RegionTransform (transforms.cr:191-222) into (offset, shape, stride)."""
+    off = offset
+    nshape, nstride = [], []
+    for i in range(region.proper_dimensions):
+        if region.proper_shape[i] > 0:
+            off += region.first[i] * stride[i]
+        if region.drop and region.degeneracy[i]:
+            continue
+        nshape.append(region.proper_shape[i])
+        nstride.append(region.step[i] * stride[i])
+    if not nshape:  # every axis dropped: shape [size] (index_region.cr:304-317)
+        nshape, nstride = [shape_to_size(region.proper_shape)], [0]
+    return off, nshape, nstride
+
+
+def _affine_permute(offset, shape, stride, order):
+    """PermuteTransform (transforms.cr:224-271): view axis i is source axis order[i]."""
+    return offset, [shape[o] for o in order], [stride[o] for o in order]
+
+
+def _affine_reverse(offset, shape, stride):
+    """ReverseTransform (transforms.cr:273-305): every axis reversed."""
+    off = offset
+    for n, s in zip(shape, stride):
+        if n > 0:
+            off += (n - 1) * s
+    return off, list(shape), [-s for s in stride]
+
+
+def _affine_reshape(offset, shape, stride, new_shape):
+    """ReshapeTransform (transforms.cr:118-189) when it stays affine: the lexicographic
+    order of the view is regrouped without moving elements.  Returns None when the
+    view's layout cannot express the new shape with strides."""
+    old = [(n, s) for n, s in zip(shape, stride) if n != 1]
+    new = list(new_shape)
+    if shape_to_size(new) == 0 or shape_to_size(list(shape)) == 0:
+        return offset, new, _row_major(new)
+    nst = [0] * len(new)
+    oi, ni = 0, 0
+    on, nn = len(old), len(new)
+    while ni < nn and oi < on:
+        if new[ni] == 1:
+            nst[ni] = 0
+            ni += 1
+            continue
+        # group old axes [oi, oj) with new axes [ni, nj) of equal element count
+        op, np_ = old[oi][0], new[ni]
+        oj, nj = oi + 1, ni + 1
+        while op != np_:
+            if op < np_:
+                if oj >= on:
+                    return None
+                op *= old[oj][0]
+                oj += 1
+            else:
+                if nj >= nn:
+                    return None
+                np_ *= new[nj]
+                nj += 1
+        for k in range(oi, oj - 1):  # the old group must be contiguous in itself
+            if old[k][1] != old[k + 1][1] * old[k + 1][0]:
+                return None
+        s = old[oj - 1][1]
+        for k in range(nj - 1, ni - 1, -1):
+            nst[k] = s
+            s *= new[k]
+        oi, ni = oj, nj
+    while ni < nn:
+        if new[ni] != 1:
+            return None
+        nst[ni] = 0
+        ni += 1
+    return offset, new, nst
+
+
+# =========================================================== common surface
+class _Indexable:
+    """Shared MultiIndexable surface (src/multi_indexable.cr)."""
+
+    dtype = A.F32
+
+    # ------------------------------------------------ required by subclasses
+    def _desc(self):
+        """(buffer, offset, shape, stride) of an affine operand."""
+        raise NotImplementedError
+
+    # -------------------------------------------------------------- shape
+    @property
+    def shape(self):
+        """A copy of the shape (multi_indexable.cr:45-47)."""
+        return list(self._shape)
+
+    @property
+    def size(self):
+        return shape_to_size(self._shape)
+
+    @property
+    def dimensions(self):
+        return len(self._shape)
+
+    def is_empty(self):
+        return self.size == 0
+
+    def is_scalar(self):
+        return self.size == 1
+
+    @property
+    def np_dtype(self):
+        return _NP[self.dtype]
+
+    # -------------------------------------------------------- materialise
+    def to_cu(self):
+        """Materialises into a new contiguous CuNArray (one gather kernel)."""
+        out = CuNArray.empty(self._shape, self.dtype)
+        _copy_into(out._view(), self._cview())
+        return out
+
+    def to_narr(self):
+        """Downloads into a numpy array (the host-side NArray)."""
+        a = self if isinstance(self, CuNArray) else self.to_cu()
+        host = np.empty(a._shape, dtype=_NP[a.dtype])
+        if host.nbytes:
+            A.check(lib().phcu_download(host.ctypes.data, a._buf.ptr, host.nbytes), "phcu_download")
+        return host
+
+    to_numpy = to_narr
+
+    def _cview(self):
+        buf, off, shape, stride = self._desc()
+        return _make_view(buf, self.dtype, off, shape, stride)
+
+    # -------------------------------------------------------------- access
+    def get(self, *coord):
+        """MultiIndexable#get (canonicalised, bounds-checked) -> Python scalar."""
+        from .region import canonicalize_index
+
+        coord = normalise_literal(coord)
+        if len(coord) != self.dimensions:
+            raise DimensionError("Could not canonicalize coordinate %r to fit in shape %r" % (coord, self.shape))
+        coord = [canonicalize_index(c, n) for c, n in zip(coord, self._shape)]
+        return self._fetch_element(coord)
+
+    get_element = get
+
+    def _fetch_element(self, coord):
+        buf, off, shape, stride = self._desc()
+        idx = off + sum(c * s for c, s in zip(coord, stride))
+        host = np.empty(1, dtype=_NP[self.dtype])
+        es = host.itemsize
+        A.check(lib().phcu_download(host.ctypes.data, buf.ptr + idx * es, es), "phcu_download")
+        return host[0].item()
+
+    def get_chunk(self, *region_literal, drop=True):
+        """MultiIndexable#get_chunk / #[] (multi_indexable.cr:354-356, 523-525)."""
+        lits = normalise_literal(region_literal)
+        if len(lits) == 1 and isinstance(lits[0], IndexRegion):
+            region = lits[0]
+            check_region_fits(region, self._shape)
+        else:
+            region = IndexRegion.new(lits, self._shape, drop)
+        return self._unsafe_fetch_chunk(region)
+
+    def __getitem__(self, key):
+        if not isinstance(key, tuple):
+            key = (key,)
+        return self.get_chunk(*key)
+
+    def get_available(self, *region_literal, drop=True):
+        """MultiIndexable#get_available (multi_indexable.cr:397-413)."""
+        lits = normalise_literal(region_literal)
+        region = IndexRegion.trimmed(lits, self._shape, bound_shape=self._shape, drop=drop)
+        return self._unsafe_fetch_chunk(region)
+
+    def has_region(self, *region_literal):
+        try:
+            IndexRegion.new(normalise_literal(region_literal), self._shape)
+            return True
+        except (IndexError, DimensionError):
+            return False
+
+    def _unsafe_fetch_chunk(self, region):
+        # default (NArray): a copy (n_array.cr:450-453)
+        return self._region_view(region).to_cu()
+
+    def _region_view(self, region):
+        buf, off, shape, stride = self._desc()
+        o, s, st = _affine_region(off, shape, stride, region)
+        return CuView(self._base(), buf, self.dtype, o, s, st)
+
+    def _base(self):
+        return self
+
+    # --------------------------------------------------------------- views
+    def view(self, *region):
+        """MultiIndexable#view (multi_indexable.cr:881-887): an aliasing CuView."""
+        buf, off, shape, stride = self._desc()
+        v = CuView(self._base(), buf, self.dtype, off, shape, stride)
+        lits = normalise_literal(region)
+        if lits:
+            return v._restrict(lits)
+        return v
+
+    def process(self, fn=None):
+        """MultiIndexable#process (multi_indexable.cr:889-895): a lazy CuProcView.
+        `fn` receives a symbolic element and returns an expression built with
+        infix operators, e.g. x.process(lambda e: (e + 4) ** 2)."""
+        pv = CuProcView._leaf(self)
+        return pv.process(fn) if fn is not None else pv
+
+    # --------------------------------------------------- iteration (host)
+    def each(self):
+        return iter(self.to_narr().reshape(-1).tolist())
+
+    def fast_each(self):
+        return self.each()
+
+    def each_with_coord(self):
+        a = self.to_narr()
+        for idx in np.ndindex(*a.shape):
+            yield a[idx].item(), list(idx)
+
+    def to_a(self):
+        return self.to_narr().reshape(-1).tolist()
+
+    # -------------------------------------------------------------- slices
+    def each_slice(self, axis=0):
+        """MultiIndexable#each_slice (multi_indexable.cr:742-748): axis `axis` fixed
+        and dropped, in increasing index order."""
+        if not (0 <= axis < self.dimensions):
+            raise IndexError("axis %d is not present in a %d-dimensional MultiIndexable" % (axis, self.dimensions))
+        for i in range(self._shape[axis]):
+            lits = [slice(None)] * self.dimensions
+            lits[axis] = i
+            yield self.get_chunk(*lits)
+
+    def slices(self, axis=0):
+        return list(self.each_slice(axis))
+
+    # ------------------------------------------- materialising transforms
+    def permute(self, *order):
+        """MultiIndexable#permute (multi_indexable.cr:795-803): a permuted copy."""
+        return self.view().permute(*order).to_cu()
+
+    def reverse(self):
+        return self.view().reverse().to_cu()
+
+    def reshape(self, *new_shape):
+        return self.view().reshape(*new_shape).to_cu()
+
+    # ------------------------------------------------------------ compare
+    def equals(self, other):
+        if self.shape != other.shape:
+            return False
+        return bool(np.array_equal(self.to_narr(), other.to_narr()))
+
+    def __eq__(self, other):
+        """MultiIndexable#== (multi_indexable.cr:74-84): same type, shape and elements."""
+        if not isinstance(other, _Indexable):
+            return False
+        return self.equals(other)
+
+    __hash__ = None
+
+    def eq(self, other):
+        """Elementwise equality -> Bool array (multi_indexable.cr:899-913)."""
+        if isinstance(other, _Indexable) and self.shape != other.shape:
+            raise DimensionError("Cannot compute the element-wise equality between this MultiIndexable (shape: %r) "
+                                 "and the one provided (shape: %r)." % (self.shape, other.shape))
+        return self._binary(A.OP_EQ, other)
+
+    # ------------------------------------------------------------ infix ops
+    def _binary(self, op, other, reflected=False):
+        if isinstance(other, CuProcView):
+            me = CuProcView._leaf(self)
+            return me._binary(op, other, reflected)
+        if isinstance(other, _Indexable):
+            a, b = (other, self) if reflected else (self, other)
+            if a._shape != b._shape:
+                name = _OP_NAMES.get(op, str(op))
+                if a.is_scalar() or b.is_scalar():
+                    raise ShapeError("The shape of this MultiIndexable (%r) does not match the shape of the one "
+                                     "provided (%r), so '%s' cannot be applied element-wise. Did you mean to call "
+                                     "to_scalar on one of the arguments?" % (a.shape, b.shape, name))
+                raise ShapeError("The shape of this MultiIndexable (%r) does not match the shape of the one provided "
+                                 "(%r), so '%s' cannot be applied element-wise." % (a.shape, b.shape, name))
+            tout = result_dtype(op, a.dtype, b.dtype)
+            out = CuNArray.empty(self._shape, tout)
+            A.check(lib().phcu_binary(op, ctypes.byref(a._cview()), ctypes.byref(b._cview()),
+                                      ctypes.byref(out._view())), "phcu_binary")
+            _after(op, a.dtype, b.dtype)
+            return out
+        # scalar operand
+        st = scalar_dtype(other)
+        ta, tb = (st, self.dtype) if reflected else (self.dtype, st)
+        tout = result_dtype(op, ta, tb)
+        out = CuNArray.empty(self._shape, tout)
+        s = A.Scalar()
+        s.dtype = st
+        if _is_float(st):
+            s.v.f = float(other)
+        else:
+            s.v.i = int(other)
+        A.check(lib().phcu_binary_scalar(op, ctypes.byref(self._cview()), ctypes.byref(s), 1 if reflected else 0,
+                                         ctypes.byref(out._view())), "phcu_binary_scalar")
+        _after(op, ta, tb)
+        return out
+
+    def __add__(self, o): return self._binary(A.OP_ADD, o)
+    def __radd__(self, o): return self._binary(A.OP_ADD, o, True)
+    def __sub__(self, o): return self._binary(A.OP_SUB, o)
+    def __rsub__(self, o): return self._binary(A.OP_SUB, o, True)
+    def __mul__(self, o): return self._binary(A.OP_MUL, o)
+    def __rmul__(self, o): return self._binary(A.OP_MUL, o, True)
+    def __truediv__(self, o): return self._binary(A.OP_DIV, o)
+    def __rtruediv__(self, o): return self._binary(A.OP_DIV, o, True)
+    def __floordiv__(self, o): return self._binary(A.OP_FLOORDIV, o)
+    def __rfloordiv__(self, o): return self._binary(A.OP_FLOORDIV, o, True)
+    def __mod__(self, o): return self._binary(A.OP_MOD, o)
+    def __rmod__(self, o): return self._binary(A.OP_MOD, o, True)
+    def __pow__(self, o): return self._binary(A.OP_POW, o)
+    def __rpow__(self, o): return self._binary(A.OP_POW, o, True)
+    def __and__(self, o): return self._binary(A.OP_AND, o)
+    def __rand__(self, o): return self._binary(A.OP_AND, o, True)
+    def __or__(self, o): return self._binary(A.OP_OR, o)
+    def __ror__(self, o): return self._binary(A.OP_OR, o, True)
+    def __xor__(self, o): return self._binary(A.OP_XOR, o)
+    def __rxor__(self, o): return self._binary(A.OP_XOR, o, True)
+    def __gt__(self, o): return self._binary(A.OP_GT, o)
+    def __lt__(self, o): return self._binary(A.OP_LT, o)
+    def __ge__(self, o): return self._binary(A.OP_GE, o)
+    def __le__(self, o): return self._binary(A.OP_LE, o)
+
+    def wadd(self, o):
+        """Crystal `&+` (wrapping addition)."""
+        return self._binary(A.OP_WADD, o)
+
+    def wsub(self, o):
+        """Crystal `&-`."""
+        return self._binary(A.OP_WSUB, o)
+
+    def wmul(self, o):
+        """Crystal `&*`."""
+        return self._binary(A.OP_WMUL, o)
+
+    def wpow(self, o):
+        """Crystal `&**`."""
+        return self._binary(A.OP_WPOW, o)
+
+    def cmp(self, o):
+        """Crystal `<=>` elementwise -> Int32 array."""
+        return self._binary(A.OP_CMP, o)
+
+    def _unary(self, uop):
+        if self.dtype == A.BOOL or (uop == A.UOP_NOT and not _is_int(self.dtype)):
+            raise NotImplementedError("unary operator not defined for %s" % A.DTYPE_NAMES[self.dtype])
+        out = CuNArray.empty(self._shape, self.dtype)
+        A.check(lib().phcu_unary(uop, ctypes.byref(self._cview()), ctypes.byref(out._view())), "phcu_unary")
+        if uop == A.UOP_NEG and _is_int(self.dtype) and config.eager_errors:
+            check_errors()
+        return out
+
+    def __neg__(self): return self._unary(A.UOP_NEG)
+    def __pos__(self): return self._unary(A.UOP_POS)
+    def __invert__(self): return self._unary(A.UOP_NOT)
+
+    # ---------------------------------------------------------- reductions
+    def _reduce(self, op, axis, out_dtype=None):
+        if self.dtype == A.BOOL and op == A.RED_SUM:
+            raise NotImplementedError("sum of Bool")
+        src = self
+        if axis is None:
+            n = self.size
+            if n == 0:
+                if op == A.RED_SUM:
+                    return _NP[self.dtype](0).item()
+                raise EmptyError("Empty enumerable")
+            oshape = [1]
+        else:
+            if axis < 0:
+                axis += self.dimensions
+            if not (0 <= axis < self.dimensions):
+                raise IndexError("axis %d is not present in a %d-dimensional MultiIndexable" % (axis, self.dimensions))
+            if self._shape[axis] == 0 and op != A.RED_SUM:
+                raise EmptyError("Empty enumerable")
+            oshape = self._shape[:axis] + self._shape[axis + 1:]
+        if out_dtype is None:
+            out_dtype = A.I32 if op in (A.RED_ARGMAX, A.RED_ARGMIN) and axis is not None else (
+                A.I64 if op in (A.RED_ARGMAX, A.RED_ARGMIN) else self.dtype)
+        out = CuNArray.empty(oshape if oshape else [1], out_dtype)
+        A.check(lib().phcu_reduce(op, ctypes.byref(src._cview()), -1 if axis is None else axis,
+                                  ctypes.byref(out._view())), "phcu_reduce")
+        if op == A.RED_SUM and _is_int(self.dtype) and config.eager_errors:
+            check_errors()
+        if axis is None:
+            v = out.to_narr().reshape(-1)[0].item()
+            if op in (A.RED_ARGMAX, A.RED_ARGMIN):
+                return list(np.unravel_index(int(v), self._shape)) if self._shape else [int(v)]
+            return v
+        if not oshape:
+            return out.to_narr().reshape(-1)[0].item()
+        return out
+
+    def sum(self, axis=None, dtype=None):
+        """Enumerable#sum (axis=None) or the slices(axis) fold; Float32 sums are
+        compensated on the device (pass dtype=Float64 for an FP64 result)."""
+        return self._reduce(A.RED_SUM, axis, dtype)
+
+    def max(self, axis=None):
+        return self._reduce(A.RED_MAX, axis)
+
+    def min(self, axis=None):
+        return self._reduce(A.RED_MIN, axis)
+
+    def argmax(self, axis=None):
+        """README.md:56-61 idiom: first maximum wins; axis=None returns its coordinate."""
+        return self._reduce(A.RED_ARGMAX, axis)
+
+    def argmin(self, axis=None):
+        return self._reduce(A.RED_ARGMIN, axis)
+
+    def __repr__(self):
+        return "%s(%s, %s)" % (type(self).__name__, "x".join(map(str, self._shape)), A.DTYPE_NAMES[self.dtype])
+
+
+_OP_NAMES = {A.OP_ADD: "+", A.OP_SUB: "-", A.OP_MUL: "*", A.OP_DIV: "/", A.OP_FLOORDIV: "//", A.OP_MOD: "%",
+             A.OP_POW: "**", A.OP_WADD: "&+", A.OP_WSUB: "&-", A.OP_WMUL: "&*", A.OP_WPOW: "&**",
+             A.OP_AND: "&", A.OP_OR: "|", A.OP_XOR: "^", A.OP_GT: ">", A.OP_LT: "<", A.OP_GE: ">=",
+             A.OP_LE: "<=", A.OP_CMP: "<=>", A.OP_EQ: "=="}
+
+
+def _can_raise(op, ta, tb):
+    if _is_int(ta) and _is_int(tb):
+        return op in (A.OP_ADD, A.OP_SUB, A.OP_MUL, A.OP_FLOORDIV, A.OP_MOD, A.OP_POW, A.OP_WPOW)
+    return op == A.OP_MOD
+
+
+def _after(op, ta, tb):
+    if config.eager_errors and _can_raise(op, ta, tb):
+        check_errors()
+
+
+def _copy_into(dst_view, src_view):
+    A.check(lib().phcu_copy(ctypes.byref(dst_view), ctypes.byref(src_view)), "phcu_copy")
+
+
+# ================================================================ CuNArray
+class CuNArray(_Indexable):
+    """Device-resident NArray (src/n_array.cr:15-913): contiguous row-major buffer."""
+
+    def __init__(self, shape, dtype, buf=None):
+        shape = [int(s) for s in shape]
+        for s in shape:
+            if s < 0:
+                raise DimensionError("Cannot create NArray: One or more of the provided dimensions was negative.")
+        self._shape = shape
+        self.dtype = dtype
+        n = shape_to_size(shape) if shape else 1
+        self._buf = buf if buf is not None else _Buffer(n * A.DTYPE_SIZE[dtype])
+
+    # --------------------------------------------------------- constructors
+    @classmethod
+    def empty(cls, shape, dtype=A.F32):
+        return cls(list(shape), dtype)
+
+    @classmethod
+    def of_buffer(cls, shape, buffer):
+        """NArray.of_buffer (n_array.cr:76-79): shape + lexicographic buffer (numpy)."""
+        buffer = np.ascontiguousarray(buffer)
+        shape = list(shape)
+        if shape_to_size(shape) != buffer.size:
+            raise ShapeError("Cannot create NArray: Given shape does not match number of elements in buffer.")
+        a = cls(shape, dtype_of_numpy(buffer.dtype))
+        if buffer.nbytes:
+            A.check(lib().phcu_upload(a._buf.ptr, buffer.ctypes.data, buffer.nbytes), "phcu_upload")
+            A.call("phcu_sync")
+        return a
+
+    @classmethod
+    def from_numpy(cls, arr):
+        arr = np.asarray(arr)
+        return cls.of_buffer(list(arr.shape), arr)
+
+    @classmethod
+    def new(cls, nested):
+        """NArray.new(nested array) / NArray[...]."""
+        return cls.from_numpy(np.asarray(nested))
+
+    @classmethod
+    def fill(cls, shape, value, dtype=None):
+        """NArray.fill (n_array.cr:230-232)."""
+        t = dtype if dtype is not None else scalar_dtype(value)
+        a = cls(list(shape), t)
+        a._fill_view(a._view(), value)
+        return a
+
+    @classmethod
+    def build(cls, shape, fn):
+        """NArray.build (n_array.cr:111-116): the block runs on the host, then uploads."""
+        shape = list(shape)
+        vals = [fn(list(c), i) for i, c in enumerate(np.ndindex(*shape))] if shape_to_size(shape) else []
+        arr = np.array(vals).reshape(shape) if vals else np.zeros(shape, dtype=np.int32)
+        return cls.of_buffer(shape, arr)
+
+    def clone(self):
+        out = CuNArray.empty(self._shape, self.dtype)
+        _copy_into(out._view(), self._view())
+        return out
+
+    # ------------------------------------------------------------- layout
+    def _desc(self):
+        return self._buf, 0, list(self._shape), _row_major(self._shape)
+
+    def _view(self):
+        return _make_view(self._buf, self.dtype, 0, self._shape, _row_major(self._shape))
+
+    @property
+    def buffer(self):
+        return self.to_narr().reshape(-1)
+
+    def reshape(self, *new_shape):
+        """NArray#reshape (n_array.cr:429-437): same buffer, new shape."""
+        new_shape = normalise_literal(new_shape)
+        if shape_to_size(new_shape) != self.size:
+            raise ShapeError("Cannot create NArray: Given shape does not match number of elements in buffer.")
+        return CuNArray(new_shape, self.dtype, self._buf)
+
+    def flatten(self):
+        return self.reshape(self.size)
+
+    # ------------------------------------------------------------ writing
+    def _fill_view(self, view, value):
+        s = A.Scalar()
+        s.dtype = self.dtype
+        v = _cast_scalar(value, self.dtype)
+        if _is_float(self.dtype):
+            s.v.f = float(v)
+        else:
+            s.v.i = int(v)
+        A.check(lib().phcu_fill(ctypes.byref(view), ctypes.byref(s)), "phcu_fill")
+
+    def set_chunk(self, *args):
+        """MultiWritable#set_chunk / #[]= (multi_writable.cr:55-84)."""
+        *lits, src = args
+        lits = normalise_literal(lits)
+        if len(lits) == 1 and isinstance(lits[0], IndexRegion):
+            region = lits[0]
+        else:
+            region = IndexRegion.new(lits, self._shape)
+        _write_region(self, region, src)
+
+    def __setitem__(self, key, value):
+        if not isinstance(key, tuple):
+            key = (key,)
+        if len(key) == 1 and isinstance(key[0], _Indexable) and key[0].dtype == A.BOOL:
+            return self.set_mask(key[0], value)
+        self.set_chunk(*key, value)
+
+    def set_element(self, coord, value):
+        from .region import canonicalize_index
+
+        coord = [canonicalize_index(c, n) for c, n in zip(coord, self._shape)]
+        if len(coord) != self.dimensions:
+            raise DimensionError("coordinate rank mismatch")
+        reg = IndexRegion.new(coord, self._shape, drop=False)
+        _write_region(self, reg, value)
+
+    def set_mask(self, mask, value):
+        """MultiWritable#set_mask (multi_writable.cr:127-172): masked write,
+        evaluated as one select kernel: out = mask ? value : self."""
+        if mask.shape != self._shape:
+            raise ShapeError("Cannot perform masking: mask shape %r does not match array shape %r."
+                             % (mask.shape, self._shape))
+        if isinstance(value, _Indexable) and value.shape != self._shape:
+            raise ShapeError("Cannot perform masking: source shape %r does not match array shape %r."
+                             % (value.shape, self._shape))
+        m = mask.to_narr()
+        cur = self.to_narr()
+        v = value.to_narr() if isinstance(value, _Indexable) else value
+        new = np.where(m, v, cur).astype(_NP[self.dtype])
+        A.check(lib().phcu_upload(self._buf.ptr, new.ctypes.data, new.nbytes), "phcu_upload")
+        A.call("phcu_sync")
+
+    def mutable_view(self, *region):
+        """MultiIndexable::Mutable#mutable_view (mutable.cr:6-12)."""
+        v = CuMutableView(self, self._buf, self.dtype, 0, list(self._shape), _row_major(self._shape))
+        lits = normalise_literal(region)
+        return v._restrict(lits) if lits else v
+
+    def map_inplace(self, fn):
+        """Mutable#map! with a symbolic block: self = fn(self), one kernel."""
+        pv = CuProcView._leaf(self).process(fn)
+        pv._eval_into(self._view(), self.dtype)
+        return self
+
+
+def _write_region(target, region, src):
+    """unsafe_set_chunk (n_array.cr:484-500; multi_writable.cr:29-44) with a
+    device source (gather/scatter kernel) or a scalar (fill kernel)."""
+    if isinstance(src, CuProcView):
+        src = src.to_cu()
+    buf, off, shape, stride = target._desc()
+    o, s, st = _affine_region(off, shape, stride, region)
+    dview = _make_view(buf, target.dtype, o, s, st)
+    if isinstance(src, _Indexable):
+        if not compatible_shapes(src.shape, region.shape):
+            raise ShapeError("Cannot substitute %s: the given %s has shape %r, but region %r has shape %r."
+                             % (type(src).__name__, type(src).__name__, src.shape, region, region.shape))
+        if src.dtype != target.dtype:
+            src = src.to_cu()._astype(target.dtype)
+        _copy_into(dview, src._cview())
+    else:
+        sv = A.Scalar()
+        sv.dtype = target.dtype
+        v = _cast_scalar(src, target.dtype)
+        if _is_float(target.dtype):
+            sv.v.f = float(v)
+        else:
+            sv.v.i = int(v)
+        A.check(lib().phcu_fill(ctypes.byref(dview), ctypes.byref(sv)), "phcu_fill")
+
+
+def _astype(self, t):
+    if t == self.dtype:
+        return self
+    out = CuNArray.empty(self._shape, t)
+    pv = CuProcView._leaf(self)
+    pv._expr = ("cvt", t, pv._expr)
+    pv.dtype = t
+    pv._eval_into(out._view(), t)
+    return out
+
+
+CuNArray._astype = _astype
+
+
+# ================================================================== CuView
+class CuView(_Indexable):
+    """Lazy aliasing view over a device buffer (src/view.cr): the transform
+    chain is folded into one affine map (offset, shape, stride)."""
+
+    def __init__(self, src, buf, dtype, offset, shape, stride):
+        self._src = src
+        self._buf = buf
+        self.dtype = dtype
+        self._off = int(offset)
+        self._shape = [int(x) for x in shape]
+        self._stride = [int(x) for x in stride]
+
+    def _desc(self):
+        return self._buf, self._off, list(self._shape), list(self._stride)
+
+    def _base(self):
+        return self._src
+
+    def _new(self, off, shape, stride):
+        return type(self)(self._src, self._buf, self.dtype, off, shape, stride)
+
+    def clone(self):
+        return self._new(self._off, self._shape, self._stride)
+
+    def _restrict(self, lits):
+        """View#restrict_to (view.cr:43-56) with a literal or an IndexRegion."""
+        if len(lits) == 1 and isinstance(lits[0], IndexRegion):
+            region = lits[0]
+        else:
+            region = IndexRegion.new(lits, self._shape)
+        o, s, st = _affine_region(self._off, self._shape, self._stride, region)
+        return self._new(o, s, st)
+
+    def view(self, *region):
+        """View#view (view.cr:36-40): a new view composed with `region`."""
+        lits = normalise_literal(region)
+        v = CuView(self._src, self._buf, self.dtype, self._off, self._shape, self._stride)
+        return v._restrict(lits) if lits else v
+
+    def _unsafe_fetch_chunk(self, region):
+        """View#unsafe_fetch_chunk (view.cr:105-107): another view, no copy."""
+        o, s, st = _affine_region(self._off, self._shape, self._stride, region)
+        return CuView(self._src, self._buf, self.dtype, o, s, st)
+
+    def permute(self, *order):
+        """View#permute (view.cr:72-89); no argument reverses the axis order."""
+        order = normalise_literal(order)
+        if not order:
+            order = list(range(self.dimensions - 1, -1, -1))
+        bad = [a for a in order if a < 0 or a >= self.dimensions]
+        if bad:
+            raise IndexError("Could not use pattern %r to permute: Axis %d is not present in a %d-dimensional "
+                             "MultiIndexable" % (order, bad[0], self.dimensions))
+        return self._new(*_affine_permute(self._off, self._shape, self._stride, order))
+
+    def reverse(self):
+        """View#reverse (view.cr:96-103): every axis reversed."""
+        return self._new(*_affine_reverse(self._off, self._shape, self._stride))
+
+    def reshape(self, *new_shape):
+        """View#reshape (view.cr:58-70)."""
+        new_shape = [int(x) for x in normalise_literal(new_shape)]
+        if shape_to_size(new_shape) != self.size:
+            raise ShapeError("Cannot change shape from %s (%d elements) to %s (%d elements) because reshape cannot "
+                             "add or remove elements." % ("x".join(map(str, self._shape)), self.size,
+                                                          "x".join(map(str, new_shape)), shape_to_size(new_shape)))
+        r = _affine_reshape(self._off, self._shape, self._stride, new_shape)
+        if r is not None:
+            return self._new(*r)
+        if isinstance(self, CuMutableView):
+            raise NotImplementedError("a writable reshape of this strided view is not affine")
+        # the layout cannot express the new shape: materialise (reads now, not lazily)
+        mat = self.to_cu().reshape(new_shape)
+        return CuView(mat, mat._buf, self.dtype, 0, new_shape, _row_major(new_shape))
+
+    def to_narr(self):
+        return self.to_cu().to_narr()
+
+
+class CuMutableView(CuView):
+    """Writable view (src/mutable_view.cr): writes land in the source buffer."""
+
+    def view(self, *region):
+        """MutableView#view (mutable_view.cr:20-24) returns a read-only view."""
+        v = CuView(self._src, self._buf, self.dtype, self._off, self._shape, self._stride)
+        lits = normalise_literal(region)
+        return v._restrict(lits) if lits else v
+
+    def mutable_view(self, *region):
+        lits = normalise_literal(region)
+        v = self.clone()
+        return v._restrict(lits) if lits else v
+
+    def set_chunk(self, *args):
+        *lits, src = args
+        lits = normalise_literal(lits)
+        if len(lits) == 1 and isinstance(lits[0], IndexRegion):
+            region = lits[0]
+        else:
+            region = IndexRegion.new(lits, self._shape)
+        _write_region(self, region, src)
+
+    def __setitem__(self, key, value):
+        if not isinstance(key, tuple):
+            key = (key,)
+        self.set_chunk(*key, value)
+
+
+# ============================================================= CuProcView
+class _Sym:
+    """Symbolic element handed to process() blocks."""
+
+    __slots__ = ("expr", "dtype")
+
+    def __init__(self, expr, dtype):
+        self.expr, self.dtype = expr, dtype
+
+    def _bin(self, op, other, reflected=False):
+        if isinstance(other, _Sym):
+            oe, ot = other.expr, other.dtype
+        else:
+            ot = scalar_dtype(other)
+            oe = ("const", other, ot)
+        a, ta, b, tb = (oe, ot, self.expr, self.dtype) if reflected else (self.expr, self.dtype, oe, ot)
+        t = result_dtype(op, ta, tb)
+        return _Sym(("bin", op, a, b, ta, tb, t), t)
+
+    def __add__(self, o): return self._bin(A.OP_ADD, o)
+    def __radd__(self, o): return self._bin(A.OP_ADD, o, True)
+    def __sub__(self, o): return self._bin(A.OP_SUB, o)
+    def __rsub__(self, o): return self._bin(A.OP_SUB, o, True)
+    def __mul__(self, o): return self._bin(A.OP_MUL, o)
+    def __rmul__(self, o): return self._bin(A.OP_MUL, o, True)
+    def __truediv__(self, o): return self._bin(A.OP_DIV, o)
+    def __rtruediv__(self, o): return self._bin(A.OP_DIV, o, True)
+    def __floordiv__(self, o): return self._bin(A.OP_FLOORDIV, o)
+    def __mod__(self, o): return self._bin(A.OP_MOD, o)
+    def __pow__(self, o): return self._bin(A.OP_POW, o)
+    def __and__(self, o): return self._bin(A.OP_AND, o)
+    def __or__(self, o): return self._bin(A.OP_OR, o)
+    def __xor__(self, o): return self._bin(A.OP_XOR, o)
+    def __gt__(self, o): return self._bin(A.OP_GT, o)
+    def __lt__(self, o): return self._bin(A.OP_LT, o)
+    def __ge__(self, o): return self._bin(A.OP_GE, o)
+    def __le__(self, o): return self._bin(A.OP_LE, o)
+
+    def __neg__(self):
+        return _Sym(("un", A.I_NEG, self.expr, self.dtype), self.dtype)
+
+
+class CuProcView(_Indexable):
+    """Lazy elementwise program over up to four aliasing operand views
+    (src/proc_view.cr).  process() composes blocks (proc_view.cr:32-35); infix
+    operators with views, arrays or scalars extend the program; the whole chain
+    runs as ONE kernel when it is materialised (to_cu / to_narr / a reduction)."""
+
+    def __init__(self, leaves, expr, dtype, shape):
+        self._leaves = leaves  # list of CuView
+        self._expr = expr
+        self.dtype = dtype
+        self._shape = list(shape)
+
+    @classmethod
+    def _leaf(cls, x):
+        if isinstance(x, CuProcView):
+            return x
+        buf, off, shape, stride = x._desc()
+        v = CuView(x._base(), buf, x.dtype, off, shape, stride)
+        return cls([v], ("in", 0, x.dtype), x.dtype, x.shape)
+
+    def _desc(self):
+        raise NotImplementedError("a CuProcView has no storage; materialise it with to_cu()")
+
+    def _cview(self):
+        # a temporary CuNArray would be freed (stream-ordered) before its use
+        raise NotImplementedError("materialise a CuProcView with to_cu() before passing it to a kernel")
+
+    def _fetch_element(self, coord):
+        return self.to_cu()._fetch_element(coord)
+
+    def process(self, fn):
+        sym = fn(_Sym(self._expr, self.dtype))
+        if not isinstance(sym, _Sym):
+            # constant block: broadcast the constant
+            t = scalar_dtype(sym)
+            return CuProcView(self._leaves, ("const", sym, t), t, self._shape)
+        return CuProcView(self._leaves, sym.expr, sym.dtype, self._shape)
+
+    # elementwise programs commute with index transforms: apply to every leaf
+    def _map_leaves(self, f):
+        return CuProcView([f(l) for l in self._leaves], self._expr, self.dtype, None)._fix_shape()
+
+    def _fix_shape(self):
+        self._shape = list(self._leaves[0].shape) if self._leaves else self._shape
+        return self
+
+    def view(self, *region):
+        lits = normalise_literal(region)
+        return self._map_leaves(lambda l: l.view(*lits))
+
+    def permute(self, *order):
+        return self._map_leaves(lambda l: l.permute(*order))
+
+    def reverse(self):
+        return self._map_leaves(lambda l: l.reverse())
+
+    def _unsafe_fetch_chunk(self, region):
+        return self._map_leaves(lambda l: l._unsafe_fetch_chunk(region))
+
+    def _binary(self, op, other, reflected=False):
+        leaves = list(self._leaves)
+        if isinstance(other, CuProcView):
+            if other._shape != self._shape:
+                raise ShapeError("The shape of this MultiIndexable (%r) does not match the shape of the one provided "
+                                 "(%r), so '%s' cannot be applied element-wise." % (self._shape, other._shape,
+                                                                                     _OP_NAMES.get(op)))
+            base = len(leaves)
+            leaves += other._leaves
+            oe = _shift(other._expr, base)
+            ot = other.dtype
+        elif isinstance(other, _Indexable):
+            if other.shape != self._shape:
+                raise ShapeError("The shape of this MultiIndexable (%r) does not match the shape of the one provided "
+                                 "(%r), so '%s' cannot be applied element-wise." % (self._shape, other.shape,
+                                                                                     _OP_NAMES.get(op)))
+            buf, off, shape, stride = other._desc()
+            leaves.append(CuView(other._base(), buf, other.dtype, off, shape, stride))
+            oe = ("in", len(leaves) - 1, other.dtype)
+            ot = other.dtype
+        else:
+            ot = scalar_dtype(other)
+            oe = ("const", other, ot)
+        a, ta, b, tb = (oe, ot, self._expr, self.dtype) if reflected else (self._expr, self.dtype, oe, ot)
+        t = result_dtype(op, ta, tb)
+        pv = CuProcView(leaves, ("bin", op, a, b, ta, tb, t), t, self._shape)
+        return pv._dedupe()
+
+    def _dedupe(self):
+        # identical leaf views share one input slot
+        keys, remap, leaves = {}, {}, []
+        for i, l in enumerate(self._leaves):
+            k = (l._buf.ptr if l._buf else 0, l.dtype, l._off, tuple(l._shape), tuple(l._stride))
+            if k not in keys:
+                keys[k] = len(leaves)
+                leaves.append(l)
+            remap[i] = keys[k]
+        self._expr = _remap(self._expr, remap)
+        self._leaves = leaves
+        return self
+
+    def _unary(self, uop):
+        op = {A.UOP_NEG: A.I_NEG, A.UOP_NOT: A.I_NOT, A.UOP_POS: A.I_POS}[uop]
+        return CuProcView(self._leaves, ("un", op, self._expr, self.dtype), self.dtype, self._shape)
+
+    # ------------------------------------------------------------- evaluate
+    def _eval_into(self, out_view, out_dtype):
+        expr = self._expr
+        leaves = self._leaves
+        if len(leaves) > A.MAX_INPUTS:
+            raise NotImplementedError("a fused program reads at most %d distinct views" % A.MAX_INPUTS)
+        prog, can_raise = compile_program(expr, out_dtype)
+        ins = (A.View * max(1, len(leaves)))()
+        for k, l in enumerate(leaves):
+            ins[k] = l._cview()
+        A.check(lib().phcu_eval(ctypes.byref(prog), ins, len(leaves), ctypes.byref(out_view)), "phcu_eval")
+        if can_raise and config.eager_errors:
+            check_errors()
+
+    def to_cu(self):
+        out = CuNArray.empty(self._shape, self.dtype)
+        self._eval_into(out._view(), self.dtype)
+        return out
+
+    def to_narr(self):
+        return self.to_cu().to_narr()
+
+    def _reduce(self, op, axis, out_dtype=None):
+        return self.to_cu()._reduce(op, axis, out_dtype)
+
+
+def _shift(e, base):
+    k = e[0]
+    if k == "in":
+        return ("in", e[1] + base, e[2])
+    if k == "const":
+        return e
+    if k == "bin":
+        return ("bin", e[1], _shift(e[2], base), _shift(e[3], base)) + tuple(e[4:])
+    if k == "un":
+        return ("un", e[1], _shift(e[2], base), e[3])
+    if k == "cvt":
+        return ("cvt", e[1], _shift(e[2], base))
+    return e
+
+
+def _remap(e, m):
+    k = e[0]
+    if k == "in":
+        return ("in", m[e[1]], e[2])
+    if k == "bin":
+        return ("bin", e[1], _remap(e[2], m), _remap(e[3], m)) + tuple(e[4:])
+    if k == "un":
+        return ("un", e[1], _remap(e[2], m), e[3])
+    if k == "cvt":
+        return ("cvt", e[1], _remap(e[2], m))
+    return e
+
+
+def _etype(e):
+    k = e[0]
+    if k == "in":
+        return e[2]
+    if k == "const":
+        return e[2]
+    if k == "bin":
+        return e[6]
+    if k == "un":
+        return e[3]
+    if k == "cvt":
+        return e[1]
+    raise ValueError(e)
+
+
+# ------------------------------------------------------- program compiler
+def compile_program(expr, out_dtype):
+    """Compiles an expression tree into the library's accumulator program.
+    Returns (Program, can_raise)."""
+    code = []
+    flags = {"raise": False}
+
+    def emit(op, src=0, t=0, bt=0, imm=0, fl=0):
+        if len(code) >= A.MAX_INSTR:
+            raise NotImplementedError("fused program longer than %d instructions" % A.MAX_INSTR)
+        code.append((op, src, t, bt, imm, fl))
+
+    def simple(e):
+        return e[0] in ("in", "const")
+
+    def src_of(e):
+        if e[0] == "in":
+            return e[1], e[2], 0
+        return A.SRC_IMM, e[2], _slot_bits(e[1], e[2])
+
+    def gen(e, depth):
+        k = e[0]
+        if k in ("in", "const"):
+            s, t, imm = src_of(e)
+            emit(A.I_LD, s, t, t, imm)
+            return
+        if k == "cvt":
+            gen(e[2], depth)
+            emit(A.I_CVT, 0, _etype(e[2]), 0, e[1])
+            return
+        if k == "un":
+            gen(e[2], depth)
+            if e[1] == A.I_NEG and _is_int(e[3]):
+                flags["raise"] = True
+            emit(e[1], 0, e[3])
+            return
+        _, op, l, r, ta, tb, tout = e
+        T = _compute_type(op, ta, tb)
+        int_exp = op == A.OP_POW and _is_float(ta) and _is_int(tb)
+        if _can_raise(op, ta, tb):
+            flags["raise"] = True
+        if ta == A.BOOL and tb != A.BOOL or tb == A.BOOL and ta != A.BOOL:
+            emit(A.I_LD, A.SRC_IMM, A.BOOL, A.BOOL, 0)  # Bool == number: false
+            return
+        if simple(r):
+            gen(l, depth)
+            if ta != T:
+                emit(A.I_CVT, 0, ta, 0, T)
+            s, st, imm = src_of(r)
+            emit(op, s, T, st, imm)
+        elif simple(l) and not int_exp and op != A.OP_POW:
+            gen(r, depth)
+            if tb != T:
+                emit(A.I_CVT, 0, tb, 0, T)
+            s, st, imm = src_of(l)
+            emit(op, s, T, st, imm, 1)
+        else:
+            if depth >= 2:
+                raise NotImplementedError("expression too deep for the two stash registers")
+            gen(r, depth)
+            emit(A.I_ST0 if depth == 0 else A.I_ST1, 0, tb)
+            gen(l, depth + 1)
+            if ta != T:
+                emit(A.I_CVT, 0, ta, 0, T)
+            emit(op, A.SRC_S0 if depth == 0 else A.SRC_S1, T, tb, 0)
+        rt = T
+        if op in (A.OP_GT, A.OP_LT, A.OP_GE, A.OP_LE, A.OP_EQ):
+            rt = A.BOOL
+        elif op == A.OP_CMP:
+            rt = A.I32
+        elif op == A.OP_DIV and _is_int(T):
+            rt = A.F64
+        if rt != tout:
+            emit(A.I_CVT, 0, rt, 0, tout)
+
+    gen(expr, 0)
+    et = _etype(expr)
+    if et != out_dtype:
+        emit(A.I_CVT, 0, et, 0, out_dtype)
+    P = A.Program()
+    P.n_instr = len(code)
+    P.out_type = out_dtype
+    for i, (op, src, t, bt, imm, fl) in enumerate(code):
+        c = P.code[i]
+        c.op, c.src, c.type, c.btype, c.flags = op, src, t, bt, fl
+        c.imm.i = int(imm) if imm < 2 ** 63 else int(imm) - 2 ** 64
+    return P, flags["raise"]

@@ -1,0 +1,280 @@
+"""CPU tests of the host side of the device backend: region validation
+(RangeSyntax / IndexRegion mirror), the affine view compiler, the result-type
+rules and the C-ABI surface.  No GPU needed."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, lit_from_json as L
+
+
+@pytest.fixture(scope="module")
+def reg():
+    from phase_cu import region
+
+    return region
+
+
+def test_mirror_test_ranges(reg, kats):
+    tr = kats["test_ranges"]
+    b = tr["bound"]
+    for key in ("fully_defined", "negative_indices", "implicit_bounds"):
+        for lit, (f, s, l) in tr[key]:
+            r = reg.IndexRegion.new([L(lit)], [b])
+            assert (r.first[0], r.step[0], r.last[0]) == (f, s, l)
+            assert r.shape[0] == (l - f) // s + 1
+            assert r.fits_in([b]) and not r.fits_in([max(f, l)])
+    for lit in tr["out_of_bounds"] + tr["step_conflict"]:
+        with pytest.raises(IndexError):
+            reg.IndexRegion.new([L(lit)], [b])
+    for lit in tr["empty"]:
+        assert reg.IndexRegion.new([L(lit)], [b]).size == 0
+    for lit, (f, s, l) in tr["fully_defined"]:
+        r = reg.IndexRegion.absolute([L(lit)])
+        assert (r.first[0], r.step[0], r.last[0]) == (f, s, l)
+    for lit, _ in tr["implicit_bounds"]:
+        with pytest.raises(Exception):
+            reg.IndexRegion.absolute([L(lit)])
+    for lit, _ in tr["negative_indices"]:
+        with pytest.raises(IndexError):
+            reg.IndexRegion.absolute([L(lit)])
+
+
+def test_mirror_trim(reg, kats):
+    tr = kats["test_ranges"]
+    b = tr["bound"]
+    for key in ("fully_defined", "negative_indices", "implicit_bounds"):
+        for lit, (f, s, l) in tr[key]:
+            r = reg.IndexRegion.new([L(lit)], [b])
+            if l > f:
+                r.trim([l])
+                assert (r.first[0], r.step[0], r.last[0]) == (f, s, l - s)
+            elif f > l:
+                r.trim([f])
+                assert (r.first[0], r.step[0], r.last[0]) == (f + s, s, l)
+            else:
+                r.trim([l])
+                assert r.size == 0
+
+
+def test_mirror_region_kats(reg, kats):
+    k = kats["region_multi_axis"]
+    r = reg.IndexRegion.new([L(x) for x in k["literal"]], k["bound"])
+    assert r.shape == k["shape"] and r.first == k["first"] and r.last == k["last"] and r.step == k["step"]
+    with pytest.raises(IndexError):
+        reg.IndexRegion.new([L(x) for x in k["bad_literal"]], k["bound"])
+    k = kats["region_includes"]
+    r = reg.IndexRegion.absolute([L(x) for x in k["literal"]])
+    assert not any(r.includes(c) for c in k["excluded"])
+    assert all(r.includes(c) for c in k["included"])
+    k = kats["region_translate"]
+    r = reg.IndexRegion.absolute([L(x) for x in k["literal"]])
+    t = r.clone().translate(k["offset"])
+    assert t.local_to_absolute([3, 1]) == [a + o for a, o in zip(r.local_to_absolute([3, 1]), k["offset"])]
+    for off in k["raises"]:
+        with pytest.raises(IndexError):
+            r.clone().translate(off)
+    k = kats["region_reverse"]
+    r = reg.IndexRegion.absolute([L(x) for x in k["literal"]])
+    assert r.clone().reverse().first == k["first_after"]
+    for i, n, exp in kats["canonicalize_index"]["ok"]:
+        assert reg.canonicalize_index(i, n) == exp
+    for i, n in kats["canonicalize_index"]["raises"]:
+        with pytest.raises(IndexError):
+            reg.canonicalize_index(i, n)
+    c = kats["compatible_shapes"]
+    for a, b in zip(c["base"], c["compatible"]):
+        assert reg.compatible_shapes(a, b)
+    for a, b in zip(c["base"], c["incompatible"]):
+        assert not reg.compatible_shapes(a, b)
+
+
+def _rand_lit(rng, bound):
+    """Random region literal element (ints, ranges, steps, negatives, exclusivity)."""
+    from phase_cu.region import R
+
+    k = rng.integers(0, 6)
+    if k == 0:
+        return int(rng.integers(-bound - 2, bound + 2))
+    f = None if rng.random() < 0.3 else int(rng.integers(-bound - 1, bound + 1))
+    l = None if rng.random() < 0.3 else int(rng.integers(-bound - 1, bound + 1))
+    s = None if rng.random() < 0.4 else int(rng.choice([-4, -3, -2, -1, 1, 2, 3, 4]))
+    return R(f, l, s, bool(rng.random() < 0.4))
+
+
+def test_mirror_matches_oracle_on_random_literals(reg, ora):
+    rng = np.random.default_rng(1)
+    for _ in range(3000):
+        bound = int(rng.integers(0, 12))
+        lit = _rand_lit(rng, bound)
+        try:
+            o = ora.canonicalize_range(lit, bound)
+            oerr = None
+        except ora.OracleError as e:
+            o, oerr = None, e.code
+        try:
+            m = reg.canonicalize_range(lit, bound)
+            merr = None
+        except IndexError:
+            m, merr = None, ora.ERR_INDEX
+        assert (oerr, None if o is None else tuple(o)) == (merr, None if m is None else tuple(m)), (lit, bound)
+
+
+def _strided_gather(base, off, shape, stride):
+    flat = base.reshape(-1)
+    out = np.empty(shape, dtype=base.dtype)
+    for idx in np.ndindex(*shape):
+        out[idx] = flat[off + sum(i * s for i, s in zip(idx, stride))]
+    return out
+
+
+def test_affine_view_compiler_matches_oracle(ora):
+    """The folded (offset, shape, stride) of random view chains addresses the
+    same elements as the reference's per-element transform chain."""
+    from phase_cu import narray as N
+    from phase_cu.region import IndexRegion, R
+
+    rng = np.random.default_rng(2)
+    for trial in range(150):
+        rank = int(rng.integers(1, 5))
+        shape = [int(rng.integers(1, 6)) for _ in range(rank)]
+        base = np.arange(int(np.prod(shape)), dtype=np.int32).reshape(shape)
+        off, cur, st = 0, list(shape), N._row_major(shape)
+        chain = []
+        for _ in range(int(rng.integers(1, 4))):
+            k = rng.integers(0, 3)
+            if k == 0 and all(c > 0 for c in cur):
+                lits = []
+                for n in cur:
+                    f = int(rng.integers(0, n))
+                    l = int(rng.integers(0, n))
+                    step = int(rng.integers(1, 3)) * (1 if l >= f else -1)
+                    lits.append(R(f, l, step) if rng.random() < 0.8 else f)
+                reg_ = IndexRegion.new(lits, cur)
+                off, cur, st = N._affine_region(off, cur, st, reg_)
+                chain.append(("region", lits))
+            elif k == 1:
+                order = list(rng.permutation(len(cur)))
+                off, cur, st = N._affine_permute(off, cur, st, order)
+                chain.append(("permute", [int(o) for o in order]))
+            else:
+                off, cur, st = N._affine_reverse(off, cur, st)
+                chain.append(("reverse",))
+        v = ora.ViewOperand(base, chain)
+        assert v.shape == cur
+        assert ora.gather(v).tolist() == _strided_gather(base, off, cur, st).tolist(), chain
+
+
+def test_affine_reshape(ora):
+    from phase_cu import narray as N
+
+    base = np.arange(24, dtype=np.int32).reshape(2, 3, 4)
+    off, shape, st = N._affine_reshape(0, [2, 3, 4], [12, 4, 1], [6, 4])
+    assert _strided_gather(base, off, shape, st).tolist() == base.reshape(6, 4).tolist()
+    # a reversed view regroups without copying
+    o2, s2, t2 = N._affine_reverse(0, [2, 3, 4], [12, 4, 1])
+    r = N._affine_reshape(o2, s2, t2, [24])
+    assert _strided_gather(base, *r).tolist() == base[::-1, ::-1, ::-1].reshape(24).tolist()
+    # a stepped view cannot be flattened with strides
+    assert N._affine_reshape(0, [2, 2], [12, 2], [4]) is None
+    v = ora.ViewOperand(base, [("region", [slice(None), slice(None), slice(0, 4, 2)]), ("reshape", [2, 6])])
+    assert ora.gather(v).tolist() == base[:, :, 0:4:2].reshape(2, 6).tolist()
+
+
+def test_result_dtypes_match_oracle(ora):
+    from phase_cu import narray as N
+
+    for op in range(20):
+        for ta in range(5):
+            for tb in range(5):
+                try:
+                    o = ora.result_dtype(op, ta, tb)
+                except ora.OracleError:
+                    o = None
+                try:
+                    m = N.result_dtype(op, ta, tb)
+                except NotImplementedError:
+                    m = None
+                assert o == m, (op, ta, tb)
+
+
+def test_fastdiv_formula():
+    """The invariant-divisor multiply used by every kernel's index decomposition."""
+    rng = np.random.default_rng(3)
+    ds = [1, 2, 3, 5, 7, 64, 255, 256, 1000, 4094, 65537, 2 ** 31 - 1, 2 ** 31, 2 ** 32 - 1]
+    ds += [int(x) for x in rng.integers(1, 2 ** 32 - 1, 200)]
+    for d in ds:
+        l = 0
+        while (1 << l) < d:
+            l += 1
+        m = ((((1 << l) - d) << 32) // d + 1) & 0xFFFFFFFF
+        ns = [0, 1, d - 1, d, d + 1, 2 ** 32 - 1, 2 ** 32 - 2] + [int(x) for x in rng.integers(0, 2 ** 32, 200)]
+        for n in ns:
+            if n >= 2 ** 32:
+                continue
+            t = (n * m) >> 32
+            assert (t + n) >> l == n // d, (n, d)
+
+
+def _header_functions():
+    with open(os.path.join(ROOT, "include", "phcuda.h")) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"PHCU_API\s+int32_t\s+(phcu_\w+)\s*\(", text)))
+
+
+def test_header_and_binding_agree():
+    from phase_cu import _abi
+
+    decl = _header_functions()
+    bound = sorted(_abi.exported_names())
+    assert decl == bound
+
+
+def test_library_exports_every_declared_symbol():
+    lib_path = os.path.join(ROOT, "ph-core_gb300", "phase_cu", "_lib", "libphcuda.so")
+    if not os.path.exists(lib_path):
+        import __graft_entry__
+
+        __graft_entry__.build()
+    lib = ctypes.CDLL(lib_path)
+    missing = [n for n in _header_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_status_codes_and_enums_agree_with_oracle(ora):
+    from phase_cu import _abi
+
+    assert (_abi.ERR_SHAPE, _abi.ERR_DIM, _abi.ERR_INDEX, _abi.ERR_OVERFLOW, _abi.ERR_DIVZERO) == \
+        (ora.ERR_SHAPE, ora.ERR_DIM, ora.ERR_INDEX, ora.ERR_OVERFLOW, ora.ERR_DIVZERO)
+    assert (_abi.BOOL, _abi.I32, _abi.I64, _abi.F32, _abi.F64) == (ora.BOOL, ora.I32, ora.I64, ora.F32, ora.F64)
+    assert _abi.OP_EQ == ora.OP_EQ and _abi.RED_ARGMIN == ora.RED_ARGMIN
+    assert ctypes.sizeof(_abi.View) == 8 + 4 + 4 + 8 + 8 * 8 * 2
+    assert ctypes.sizeof(_abi.Instr) == 16
+    assert ctypes.sizeof(_abi.Program) == 8 + 16 * _abi.MAX_INSTR
+
+
+def test_program_compiler_shapes():
+    """The fused chain ((x + 4) ** 2) * y - z compiles to one short program."""
+    from phase_cu import _abi as A
+    from phase_cu import narray as N
+
+    x = ("in", 0, A.F32)
+    y = ("in", 1, A.F32)
+    z = ("in", 2, A.F32)
+    t = ("bin", A.OP_ADD, x, ("const", 4, A.I32), A.F32, A.I32, A.F32)
+    t = ("bin", A.OP_POW, t, ("const", 2, A.I32), A.F32, A.I32, A.F32)
+    t = ("bin", A.OP_MUL, t, y, A.F32, A.F32, A.F32)
+    t = ("bin", A.OP_SUB, t, z, A.F32, A.F32, A.F32)
+    P, can_raise = N.compile_program(t, A.F32)
+    ops = [P.code[i].op for i in range(P.n_instr)]
+    assert ops == [A.I_LD, A.OP_ADD, A.OP_POW, A.OP_MUL, A.OP_SUB]
+    assert not can_raise
+    # a right-nested tree uses a stash register
+    e = ("bin", A.OP_MUL, ("bin", A.OP_ADD, x, y, A.F32, A.F32, A.F32), ("bin", A.OP_SUB, z, x, A.F32, A.F32, A.F32),
+         A.F32, A.F32, A.F32)
+    P, _ = N.compile_program(e, A.F32)
+    ops = [P.code[i].op for i in range(P.n_instr)]
+    assert A.I_ST0 in ops
