@@ -275,14 +275,27 @@ typedef struct {
   int32_t axis;     /* reduce axis (REDUCE) */
   int32_t n_inputs; /* EVAL: 0..PHCU_MAX_INPUTS; REDUCE: 1 */
   int32_t prog;     /* index into the program table (EVAL) */
-  int32_t chunk;    /* elements per work item (0 = library default / tuner) */
+  int32_t chunk;    /* elements per work item (0 = library default 8192) */
+  int32_t layout;   /* 0 = planner's launch shape; 1 = the alternative (ROW for
+                       EVAL, the other of GROUP/COLUMN for REDUCE) */
+  int32_t pad;
   phcu_view_t in[PHCU_MAX_INPUTS];
   phcu_view_t out;
 } phcu_task_t;
 
-/* Runs every task.  mode 0: one persistent launch over a device work queue;
- * mode 1: one ordinary launch per task (the per-op baseline).  The tasks'
- * outputs must not alias their inputs or each other. */
+/* Plans every task once and uploads the work list; the handle is replayed by
+ * phcu_batch_launch.  The tasks' outputs must not alias their inputs or each
+ * other; buffers must outlive the handle. */
+PHCU_API int32_t phcu_batch_prepare(const phcu_task_t* tasks, int32_t n_tasks, const phcu_program_t* programs,
+                                    int32_t n_programs, void** batch);
+/* mode 0: one persistent launch over the device work queue; mode 1: one
+ * ordinary launch per task (the per-op baseline); mode 2: the per-op launches
+ * captured once in a CUDA graph and replayed. */
+PHCU_API int32_t phcu_batch_launch(void* batch, int32_t mode);
+/* Planned task count (empty tasks dropped), work items and algorithmic bytes. */
+PHCU_API int32_t phcu_batch_info(void* batch, int64_t* n_tasks, int64_t* n_items, int64_t* bytes);
+PHCU_API int32_t phcu_batch_destroy(void* batch);
+/* prepare + launch(mode) + destroy */
 PHCU_API int32_t phcu_batch_run(const phcu_task_t* tasks, int32_t n_tasks, const phcu_program_t* programs,
                        int32_t n_programs, int32_t mode);
 

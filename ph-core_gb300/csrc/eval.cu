@@ -10,8 +10,7 @@
 //          contiguous along another axis R (permuted views).  A 64x64 tile of
 //          each such input is read coalesced along R into shared memory, then
 //          read back transposed so the output is written coalesced along W.
-#include "plan.h"
-#include "program.cuh"
+#include "eval_device.cuh"
 
 namespace phcu {
 
@@ -22,153 +21,22 @@ struct EvalArgs {
 };
 
 constexpr int ROW_THREADS = 256;
-constexpr int TILE_THREADS = 256;
 
-// ------------------------------------------------------------------ ROW
 template <int NIN, int VEC>
 __global__ void __launch_bounds__(ROW_THREADS) eval_row_kernel(const __grid_constant__ EvalArgs A) {
-  const EvalPlan& p = A.plan;
-  const int rank = p.sp.rank;
-  const int W = rank - 1;
-  const uint32_t nchunks = (uint32_t)(p.sp.n / VEC);
+  const uint32_t nchunks = (uint32_t)(A.plan.sp.n / VEC);
   uint32_t st = 0;
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += gridDim.x * blockDim.x) {
-    const uint32_t e0 = c * VEC;
-    uint32_t row, col;
-    p.lendiv.divmod(e0, row, col);
-    int64_t off_out = (int64_t)col * p.out.stride[W];
-    int64_t off_in[NIN > 0 ? NIN : 1];
-#pragma unroll
-    for (int k = 0; k < NIN; k++) off_in[k] = (int64_t)col * p.in[k].stride[W];
-    // decompose the row index over the outer axes (innermost first)
-    uint32_t r = row;
-    for (int a = W - 1; a >= 0; a--) {
-      uint32_t q, x;
-      p.sp.div[a].divmod(r, q, x);
-      r = q;
-      off_out += (int64_t)x * p.out.stride[a];
-#pragma unroll
-      for (int k = 0; k < NIN; k++) off_in[k] += (int64_t)x * p.in[k].stride[a];
-    }
-    uint64_t in[NIN > 0 ? NIN : 1][VEC];
-#pragma unroll
-    for (int k = 0; k < NIN; k++) {
-      const int es = dtype_size(p.in[k].dtype);
-      load_operand<VEC>(p.in[k].base + off_in[k] * es, p.in[k].stride[W], p.in[k].dtype, p.in[k].vmode, in[k]);
-    }
-    uint64_t acc[VEC];
-    run_program<NIN, VEC>(A.prog, in, acc, st);
-    const int oes = dtype_size(p.out.dtype);
-    char* op = (char*)p.out.base + off_out * oes;
-    if (p.out.vmode == VM_VEC) {
-      store_vec<VEC>(op, p.out.dtype, acc);
-    } else {
-      store_scalar<VEC>(op, p.out.stride[W] * oes, p.out.dtype, acc);
-    }
-  }
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += gridDim.x * blockDim.x)
+    row_chunk<NIN, VEC>(A.plan, A.prog, c, st);
   if (st) report_status(A.status, st);
 }
 
-// ----------------------------------------------------------------- TILE
-// Shared memory: one TILE x (TILE+1) slot array per staged input, 8-byte slots.
 template <int NIN>
 __global__ void __launch_bounds__(TILE_THREADS) eval_tile_kernel(const __grid_constant__ EvalArgs A) {
   extern __shared__ uint64_t smem[];
-  const EvalPlan& p = A.plan;
-  const int rank = p.sp.rank;
-  const int W = rank - 1;
-  const int R = p.raxis;
-  constexpr int LD = TILE + 1;
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  constexpr int NWARP = TILE_THREADS / 32;
   uint32_t st = 0;
-
-  const uint64_t ntiles = (uint64_t)p.tiles_w * p.tiles_r * p.nbatch;
-  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    uint32_t rest, tw, tr, b;
-    p.tdiv_w.divmod((uint32_t)t, rest, tw);
-    p.tdiv_r.divmod(rest, b, tr);
-    // batch coordinates (all axes except R and W)
-    int64_t off_out = 0;
-    int64_t off_in[NIN > 0 ? NIN : 1];
-#pragma unroll
-    for (int k = 0; k < NIN; k++) off_in[k] = 0;
-    uint32_t bb = b;
-    for (int a = W - 1; a >= 0; a--) {
-      if (a == R) continue;
-      uint32_t q, x;
-      p.sp.div[a].divmod(bb, q, x);
-      bb = q;
-      off_out += (int64_t)x * p.out.stride[a];
-#pragma unroll
-      for (int k = 0; k < NIN; k++) off_in[k] += (int64_t)x * p.in[k].stride[a];
-    }
-    const int64_t r0 = (int64_t)tr * TILE, w0 = (int64_t)tw * TILE;
-    const int64_t nr = min((int64_t)TILE, p.sp.shape[R] - r0);
-    const int64_t nw = min((int64_t)TILE, p.sp.shape[W] - w0);
-
-    // phase 1: staged inputs, coalesced along R
-    int slot = 0;
-#pragma unroll
-    for (int k = 0; k < NIN; k++) {
-      if (!(p.staged & (1u << k))) continue;
-      uint64_t* tile = smem + (size_t)slot * TILE * LD;
-      slot++;
-      const int es = dtype_size(p.in[k].dtype);
-      const char* base = p.in[k].base + (off_in[k] + r0 * p.in[k].stride[R] + w0 * p.in[k].stride[W]) * es;
-#pragma unroll
-      for (int i = 0; i < TILE / NWARP; i++) {
-        const int w = warp + i * NWARP;
-#pragma unroll
-        for (int j = 0; j < TILE / 32; j++) {
-          const int r = lane + 32 * j;
-          if (w < nw && r < nr) {
-            uint64_t v[1];
-            load_scalar<1>(base + ((int64_t)r * p.in[k].stride[R] + (int64_t)w * p.in[k].stride[W]) * es, 0,
-                           p.in[k].dtype, v);
-            tile[w * LD + r] = v[0];
-          }
-        }
-      }
-    }
-    if (p.staged) __syncthreads();
-
-    // phase 2: compute and write coalesced along W
-    const int oes = dtype_size(p.out.dtype);
-    char* obase = (char*)p.out.base + (off_out + r0 * p.out.stride[R] + w0) * oes;
-#pragma unroll 4
-    for (int i = 0; i < TILE / NWARP; i++) {
-      const int r = warp + i * NWARP;
-#pragma unroll
-      for (int j = 0; j < TILE / 32; j++) {
-        const int w = lane + 32 * j;
-        if (r < nr && w < nw) {
-          uint64_t in[NIN > 0 ? NIN : 1][1];
-          int s2 = 0;
-#pragma unroll
-          for (int k = 0; k < NIN; k++) {
-            if (p.staged & (1u << k)) {
-              in[k][0] = smem[(size_t)s2 * TILE * LD + w * LD + r];
-              s2++;
-            } else {
-              const int es = dtype_size(p.in[k].dtype);
-              uint64_t v[1];
-              load_scalar<1>(p.in[k].base + (off_in[k] + (r0 + r) * p.in[k].stride[R] +
-                                             (w0 + w) * p.in[k].stride[W]) * es,
-                             0, p.in[k].dtype, v);
-              in[k][0] = v[0];
-            }
-          }
-          uint64_t acc[1];
-          run_program<NIN, 1>(A.prog, in, acc, st);
-          uint64_t o[1] = {acc[0]};
-          store_scalar<1>(obase + ((int64_t)r * p.out.stride[R] + w) * oes, 0, p.out.dtype, o);
-        }
-      }
-    }
-    if (p.staged) __syncthreads();
-  }
+  const uint64_t ntiles = (uint64_t)A.plan.tiles_w * A.plan.tiles_r * A.plan.nbatch;
+  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) tile_body<NIN>(A.plan, A.prog, t, smem, st);
   if (st) report_status(A.status, st);
 }
 
@@ -217,6 +85,15 @@ int32_t launch_eval(const EvalArgs& A) {
     case 4: return launch_nin<4>(A);
   }
   return fail(PHCU_ERR_INVALID, "too many inputs (%d > %d)", A.plan.nin, MAXIN);
+}
+
+// Launches an already planned operation (used by the batched executor's per-op replay).
+int32_t launch_eval_plan(const EvalPlan& plan, const phcu_program_t& prog) {
+  EvalArgs A;
+  A.plan = plan;
+  A.prog = prog;
+  A.status = ctx().status;
+  return launch_eval(A);
 }
 
 // ------------------------------------------------------- program checks

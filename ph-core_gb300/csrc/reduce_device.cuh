@@ -1,0 +1,407 @@
+// reduce_device.cuh -- accumulators and per-output bodies of the reductions,
+// shared by the standalone kernels (reduce.cu) and the batched executor (batch.cu).
+#pragma once
+
+#include <float.h>
+
+#include <type_traits>
+
+#include "plan.h"
+
+namespace phcu {
+
+enum RedKind { RK_SUM = 0, RK_EXT = 1 };
+
+struct Partial {
+  double v;
+  long long i;
+};
+
+struct RedArgs {
+  // input: base points at element (0,...,0) of the view
+  const char* in;
+  int32_t dtype;
+  int32_t op;
+  // output space (lexicographic over the kept axes)
+  int32_t orank;
+  int32_t krank;
+  int64_t O;
+  int64_t oshape[MAXR];
+  int64_t ostride[MAXR];  // input stride of each kept axis
+  FastDiv odiv[MAXR];
+  // reduced space (one axis, or every axis for a full reduction)
+  int64_t K;
+  int64_t kshape[MAXR];
+  int64_t kstride[MAXR];
+  FastDiv kdiv[MAXR];
+  int64_t kinner;  // stride of the innermost reduced axis
+  // splitting
+  int64_t S;
+  int64_t chunk;
+  // output
+  char* out;
+  int32_t out_dtype;
+  int32_t want_index;
+  Partial* partial;  // S x O when S > 1
+  uint32_t* status;
+};
+
+template <typename T>
+struct Lim;
+template <>
+struct Lim<float> {
+  static __device__ __forceinline__ bool nan(float x) { return x != x; }
+};
+template <>
+struct Lim<double> {
+  static __device__ __forceinline__ bool nan(double x) { return x != x; }
+};
+template <>
+struct Lim<int32_t> {
+  static __device__ __forceinline__ bool nan(int32_t) { return false; }
+};
+template <>
+struct Lim<long long> {
+  static __device__ __forceinline__ bool nan(long long) { return false; }
+};
+
+// --------------------------------------------------------- accumulators
+template <typename T>
+struct SumAcc {  // floating point: Neumaier (s, c), value s + c
+  T s, c;
+  __device__ __forceinline__ void init() { s = 0; c = 0; }
+  __device__ __forceinline__ void add(T x) {
+    T t = s + x;
+    if (fabs((double)s) >= fabs((double)x)) c = c + ((s - t) + x);
+    else c = c + ((x - t) + s);
+    s = t;
+  }
+  __device__ __forceinline__ void merge(const SumAcc& o) {
+    // TwoSum(s, o.s)
+    T t = s + o.s;
+    T bp = t - s;
+    T e = (s - (t - bp)) + (o.s - bp);
+    s = t;
+    c = (c + o.c) + e;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+  __device__ __forceinline__ void shfl(int d, unsigned mask, int w) {
+    SumAcc o;
+    o.s = __shfl_down_sync(mask, s, d, w);
+    o.c = __shfl_down_sync(mask, c, d, w);
+    merge(o);
+  }
+};
+template <>
+struct SumAcc<float> {
+  float s, c;
+  __device__ __forceinline__ void init() { s = 0.f; c = 0.f; }
+  __device__ __forceinline__ void add(float x) {
+    float t = s + x;
+    if (fabsf(s) >= fabsf(x)) c = c + ((s - t) + x);
+    else c = c + ((x - t) + s);
+    s = t;
+  }
+  __device__ __forceinline__ void merge(const SumAcc& o) {
+    float t = s + o.s;
+    float bp = t - s;
+    float e = (s - (t - bp)) + (o.s - bp);
+    s = t;
+    c = (c + o.c) + e;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+  __device__ __forceinline__ void shfl(int d, unsigned mask, int w) {
+    SumAcc o;
+    o.s = __shfl_down_sync(mask, s, d, w);
+    o.c = __shfl_down_sync(mask, c, d, w);
+    merge(o);
+  }
+};
+template <>
+struct SumAcc<int32_t> {
+  long long s;
+  __device__ __forceinline__ void init() { s = 0; }
+  __device__ __forceinline__ void add(int32_t x) { s += x; }
+  __device__ __forceinline__ void merge(const SumAcc& o) { s += o.s; }
+  __device__ __forceinline__ double value() const { return (double)s; }
+  __device__ __forceinline__ void shfl(int d, unsigned mask, int w) { s += __shfl_down_sync(mask, s, d, w); }
+};
+template <>
+struct SumAcc<long long> {
+  long long s;
+  __device__ __forceinline__ void init() { s = 0; }
+  __device__ __forceinline__ void add(long long x) { s = (long long)((unsigned long long)s + (unsigned long long)x); }
+  __device__ __forceinline__ void merge(const SumAcc& o) { add(o.s); }
+  __device__ __forceinline__ double value() const { return (double)s; }
+  __device__ __forceinline__ void shfl(int d, unsigned mask, int w) { add(__shfl_down_sync(mask, s, d, w)); }
+};
+
+template <typename T>
+struct ExtAcc {  // (v, i); i < 0 = no candidate yet
+  T v;
+  long long i;
+  __device__ __forceinline__ void init() { v = 0; i = -1; }
+  __device__ __forceinline__ static bool better(T a, long long ia, T b, long long ib, bool is_max) {
+    // is (a, ia) preferred over (b, ib)?
+    if (ia < 0) return false;
+    if (ib < 0) return true;
+    if (is_max ? (a > b) : (a < b)) return true;
+    if (a == b && ia < ib) return true;
+    return false;
+  }
+  __device__ __forceinline__ void add(T x, long long k, bool is_max) {
+    if (Lim<T>::nan(x)) return;
+    if (better(x, k, v, i, is_max)) { v = x; i = k; }
+  }
+  __device__ __forceinline__ void merge(const ExtAcc& o, bool is_max) {
+    if (better(o.v, o.i, v, i, is_max)) { v = o.v; i = o.i; }
+  }
+  __device__ __forceinline__ void shfl(int d, unsigned mask, int w, bool is_max) {
+    ExtAcc o;
+    o.v = __shfl_down_sync(mask, v, d, w);
+    o.i = __shfl_down_sync(mask, i, d, w);
+    merge(o, is_max);
+  }
+};
+
+// ------------------------------------------------------------ helpers
+__device__ __forceinline__ int64_t out_offset(const RedArgs& a, uint32_t o) {
+  int64_t off = 0;
+  for (int d = a.orank - 1; d >= 0; d--) {
+    uint32_t q, x;
+    a.odiv[d].divmod(o, q, x);
+    o = q;
+    off += (int64_t)x * a.ostride[d];
+  }
+  return off;
+}
+
+__device__ __forceinline__ int64_t k_offset(const RedArgs& a, uint32_t k) {
+  if (a.krank == 1) return (int64_t)k * a.kstride[0];
+  int64_t off = 0;
+  for (int d = a.krank - 1; d >= 0; d--) {
+    uint32_t q, x;
+    a.kdiv[d].divmod(k, q, x);
+    k = q;
+    off += (int64_t)x * a.kstride[d];
+  }
+  return off;
+}
+
+template <typename T>
+__device__ __forceinline__ T ld(const char* p) {
+  return *(const T*)p;
+}
+
+__device__ __forceinline__ void store_final(const RedArgs& a, int64_t o, double v, long long vi, bool is_int_sum, long long isum,
+                            long long index, uint32_t& st) {
+  char* p = a.out + o * dtype_size(a.out_dtype);
+  if (a.want_index) {
+    if (a.out_dtype == PHCU_I32) *(int32_t*)p = (int32_t)index;
+    else *(long long*)p = index;
+    return;
+  }
+  switch (a.out_dtype) {
+    case PHCU_F32: *(float*)p = (float)v; break;
+    case PHCU_F64: *(double*)p = v; break;
+    case PHCU_I32: {
+      long long x = is_int_sum ? isum : vi;
+      if (x != (int32_t)x) st |= PHCU_ST_OVERFLOW;
+      *(int32_t*)p = (int32_t)x;
+      break;
+    }
+    case PHCU_I64: *(long long*)p = is_int_sum ? isum : vi; break;
+  }
+}
+
+// value of the extremum as (double, long long) for storage
+template <typename T>
+__device__ __forceinline__ void ext_parts(T v, double& d, long long& l) {
+  d = (double)v;
+  l = (long long)v;
+}
+
+// Finishes one output from its accumulated result (S == 1) or stores a partial.
+template <typename T, int KIND>
+__device__ __forceinline__ void finish(const RedArgs& a, int64_t o, int64_t split, const SumAcc<T>& sacc,
+                                       const ExtAcc<T>& eacc, uint32_t& st) {
+  if (a.S > 1) {
+    Partial& P = a.partial[split * a.O + o];
+    if (KIND == RK_SUM) {
+      if constexpr (sizeof(T) >= 4 && (std::is_same<T, int32_t>::value || std::is_same<T, long long>::value)) {
+        P.v = 0;
+        P.i = (long long)sacc.s;
+      } else {
+        P.v = sacc.value();
+        P.i = 0;
+      }
+    } else {
+      P.v = (double)eacc.v;
+      P.i = eacc.i;
+      if constexpr (std::is_same<T, long long>::value) {
+        // exact value kept in the index slot's partner: store the int64 bits in v
+        P.v = __longlong_as_double((long long)eacc.v);
+      }
+    }
+    return;
+  }
+  if (KIND == RK_SUM) {
+    if constexpr (std::is_same<T, int32_t>::value || std::is_same<T, long long>::value) {
+      store_final(a, o, 0, 0, true, (long long)sacc.s, 0, st);
+    } else {
+      store_final(a, o, sacc.value(), 0, false, 0, 0, st);
+    }
+  } else {
+    long long idx = eacc.i;
+    T v = eacc.v;
+    // first element NaN (or no candidate): the scan never moves off element 0
+    const T first = ld<T>(a.in + out_offset(a, (uint32_t)o) * sizeof(T));
+    if (idx < 0 || Lim<T>::nan(first)) {
+      idx = 0;
+      v = first;
+    }
+    double d;
+    long long l;
+    ext_parts<T>(v, d, l);
+    store_final(a, o, d, l, false, 0, idx, st);
+  }
+}
+
+
+// ------------------------------------------------------ per-output bodies
+// GROUP: the G lanes of one group reduce elements [k0, k1) of output o; lane 0
+// of the group finishes (or stores the partial of split `split`).
+template <typename T, int KIND, int G>
+__device__ __forceinline__ void group_one(const RedArgs& a, int64_t o, int64_t split, int glane, unsigned gmask,
+                                          uint32_t& st) {
+  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
+  const int64_t k0 = split * a.chunk;
+  const int64_t k1 = min(a.K, k0 + a.chunk);
+  const char* base = a.in + out_offset(a, (uint32_t)o) * (int64_t)sizeof(T);
+  SumAcc<T> sacc;
+  ExtAcc<T> eacc;
+  sacc.init();
+  eacc.init();
+  int64_t k = k0 + glane;
+  for (; k + 3 * G < k1; k += 4 * G) {  // 4 independent loads in flight per lane
+    T x0 = ld<T>(base + k_offset(a, (uint32_t)k) * (int64_t)sizeof(T));
+    T x1 = ld<T>(base + k_offset(a, (uint32_t)(k + G)) * (int64_t)sizeof(T));
+    T x2 = ld<T>(base + k_offset(a, (uint32_t)(k + 2 * G)) * (int64_t)sizeof(T));
+    T x3 = ld<T>(base + k_offset(a, (uint32_t)(k + 3 * G)) * (int64_t)sizeof(T));
+    if (KIND == RK_SUM) {
+      sacc.add(x0); sacc.add(x1); sacc.add(x2); sacc.add(x3);
+    } else {
+      eacc.add(x0, k, is_max); eacc.add(x1, k + G, is_max);
+      eacc.add(x2, k + 2 * G, is_max); eacc.add(x3, k + 3 * G, is_max);
+    }
+  }
+  for (; k < k1; k += G) {
+    T x = ld<T>(base + k_offset(a, (uint32_t)k) * (int64_t)sizeof(T));
+    if (KIND == RK_SUM) sacc.add(x);
+    else eacc.add(x, k, is_max);
+  }
+#pragma unroll
+  for (int d = G / 2; d >= 1; d >>= 1) {
+    if (KIND == RK_SUM) sacc.shfl(d, gmask, G);
+    else eacc.shfl(d, gmask, G, is_max);
+  }
+  if (glane == 0) finish<T, KIND>(a, o, split, sacc, eacc, st);
+}
+
+// COLUMN: one thread reduces elements [k0, k1) of output o.
+template <typename T, int KIND>
+__device__ __forceinline__ void column_one(const RedArgs& a, int64_t o, int64_t split, uint32_t& st) {
+  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
+  const int64_t k0 = split * a.chunk;
+  const int64_t k1 = min(a.K, k0 + a.chunk);
+  const char* base = a.in + out_offset(a, (uint32_t)o) * (int64_t)sizeof(T);
+  const int64_t ks = a.kinner * (int64_t)sizeof(T);
+  SumAcc<T> sacc;
+  ExtAcc<T> eacc;
+  sacc.init();
+  eacc.init();
+  int64_t k = k0;
+  if (a.krank == 1) {
+    const char* p = base + k0 * ks;
+    for (; k + 3 < k1; k += 4, p += 4 * ks) {
+      T x0 = ld<T>(p), x1 = ld<T>(p + ks), x2 = ld<T>(p + 2 * ks), x3 = ld<T>(p + 3 * ks);
+      if (KIND == RK_SUM) {
+        sacc.add(x0); sacc.add(x1); sacc.add(x2); sacc.add(x3);
+      } else {
+        eacc.add(x0, k, is_max); eacc.add(x1, k + 1, is_max);
+        eacc.add(x2, k + 2, is_max); eacc.add(x3, k + 3, is_max);
+      }
+    }
+    for (; k < k1; k++, p += ks) {
+      T x = ld<T>(p);
+      if (KIND == RK_SUM) sacc.add(x);
+      else eacc.add(x, k, is_max);
+    }
+  } else {
+    for (; k < k1; k++) {
+      T x = ld<T>(base + k_offset(a, (uint32_t)k) * (int64_t)sizeof(T));
+      if (KIND == RK_SUM) sacc.add(x);
+      else eacc.add(x, k, is_max);
+    }
+  }
+  finish<T, KIND>(a, o, split, sacc, eacc, st);
+}
+
+// Folds the S partials of output o in split order (FP64 for sums) and stores it.
+template <typename T, int KIND>
+__device__ __forceinline__ void combine_one(const RedArgs& a, int64_t o, uint32_t& st) {
+  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
+  if (KIND == RK_SUM) {
+    if constexpr (std::is_same<T, int32_t>::value || std::is_same<T, long long>::value) {
+      long long s = 0;
+      for (int64_t j = 0; j < a.S; j++)
+        s = (long long)((unsigned long long)s + (unsigned long long)a.partial[j * a.O + o].i);
+      store_final(a, o, 0, 0, true, s, 0, st);
+    } else {
+      double s = 0.0, c = 0.0;
+      for (int64_t j = 0; j < a.S; j++) {
+        double x = a.partial[j * a.O + o].v;
+        double t = s + x;
+        if (fabs(s) >= fabs(x)) c += (s - t) + x;
+        else c += (x - t) + s;
+        s = t;
+      }
+      store_final(a, o, s + c, 0, false, 0, 0, st);
+    }
+  } else {
+    ExtAcc<T> e;
+    e.init();
+    for (int64_t j = 0; j < a.S; j++) {
+      const Partial& P = a.partial[j * a.O + o];
+      ExtAcc<T> q;
+      if constexpr (std::is_same<T, long long>::value) q.v = __double_as_longlong(P.v);
+      else q.v = (T)P.v;
+      q.i = P.i;
+      e.merge(q, is_max);
+    }
+    long long idx = e.i;
+    T v = e.v;
+    const T first = ld<T>(a.in + out_offset(a, (uint32_t)o) * (int64_t)sizeof(T));
+    if (idx < 0 || Lim<T>::nan(first)) {
+      idx = 0;
+      v = first;
+    }
+    double d;
+    long long l;
+    ext_parts<T>(v, d, l);
+    store_final(a, o, d, l, false, 0, idx, st);
+  }
+}
+
+// Host planning of one reduction (shared with the batched executor): fills
+// `a` (without scratch) and picks the launch shape.  Returns PHCU_OK, or an
+// error; *trivial is set when nothing needs to run (no outputs) and *empty_sum
+// when the output must be zero-filled (sum over an empty axis).
+struct RedShape {
+  int mode;  // 0 = GROUP, 1 = COLUMN
+  int G;
+};
+int32_t plan_reduce(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_view_t* out, int64_t target_threads,
+                    RedArgs* a, RedShape* shape, bool* trivial, bool* empty_sum);
+
+}  // namespace phcu

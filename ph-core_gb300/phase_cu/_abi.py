@@ -90,6 +90,8 @@ class Task(ctypes.Structure):
         ("n_inputs", ctypes.c_int32),
         ("prog", ctypes.c_int32),
         ("chunk", ctypes.c_int32),
+        ("layout", ctypes.c_int32),
+        ("pad", ctypes.c_int32),
         ("inp", View * MAX_INPUTS),
         ("out", View),
     ]
@@ -140,6 +142,10 @@ _SIGS = [
     ("phcu_timer_stop", [_vp, _P(ctypes.c_float)]),
     ("phcu_launch_count", [_P(ctypes.c_uint64)]),
     ("phcu_l2_flush", []),
+    ("phcu_batch_prepare", [_P(Task), ctypes.c_int32, _P(Program), ctypes.c_int32, _P(_vp)]),
+    ("phcu_batch_launch", [_vp, ctypes.c_int32]),
+    ("phcu_batch_info", [_vp, _P(ctypes.c_int64), _P(ctypes.c_int64), _P(ctypes.c_int64)]),
+    ("phcu_batch_destroy", [_vp]),
     ("phcu_batch_run", [_P(Task), ctypes.c_int32, _P(Program), ctypes.c_int32, ctypes.c_int32]),
     ("phcu_tune_n_configs", [_P(ctypes.c_int32)]),
     ("phcu_tune_features", [_P(Task), ctypes.c_int32, _P(ctypes.c_float)]),

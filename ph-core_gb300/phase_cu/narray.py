@@ -1040,11 +1040,9 @@ class CuProcView(_Indexable):
 
     # elementwise programs commute with index transforms: apply to every leaf
     def _map_leaves(self, f):
-        return CuProcView([f(l) for l in self._leaves], self._expr, self.dtype, None)._fix_shape()
-
-    def _fix_shape(self):
-        self._shape = list(self._leaves[0].shape) if self._leaves else self._shape
-        return self
+        leaves = [f(l) for l in self._leaves]
+        shape = leaves[0].shape if leaves else self._shape
+        return CuProcView(leaves, self._expr, self.dtype, shape)
 
     def view(self, *region):
         lits = normalise_literal(region)
