@@ -16,7 +16,8 @@ OUTDIR = os.path.join(HERE, "phase_cu", "_lib")
 BUILDDIR = os.path.join(HERE, "_build")
 LIBNAME = "libphcuda.so"
 
-SOURCES = ["runtime.cu", "plan.cu", "eval.cu", "reduce.cu", "stencil.cu", "batch.cu", "tuner.cu"]
+SOURCES = ["runtime.cu", "plan.cu", "eval.cu", "eval_inst_u32_lo.cu", "eval_inst_u32_hi.cu", "eval_inst_u64_lo.cu",
+           "eval_inst_u64_hi.cu", "reduce.cu", "stencil.cu", "batch.cu", "tuner.cu"]
 
 # -fmad=false: no FMA contraction anywhere, so single Float32 operations round
 # exactly as on the host; IEEE division and square root stay the default.

@@ -120,8 +120,11 @@ struct BatchArgs {
   uint64_t deadline_ns;  // global-timer budget per launch
 };
 
+template <typename S>
 __global__ void __launch_bounds__(BATCH_THREADS) batch_kernel(const __grid_constant__ BatchArgs A) {
-  extern __shared__ uint64_t tiles[];
+  extern __shared__ __align__(16) unsigned char tiles_raw[];
+  S* tiles = reinterpret_cast<S*>(tiles_raw);
+  constexpr int E = sizeof(S) == 4 ? 8 : 4;  // elements per thread per row pass
   __shared__ __align__(16) unsigned char s_plan[sizeof(EvalPlan) > sizeof(RedArgs) ? sizeof(EvalPlan)
                                                                                     : sizeof(RedArgs)];
   __shared__ __align__(16) unsigned char s_prog[sizeof(phcu_program_t)];
@@ -162,20 +165,24 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_kernel(const __grid_const
     if (kind == BK_ROW) {
       const EvalPlan& p = *reinterpret_cast<const EvalPlan*>(s_plan);
       const phcu_program_t& prog = *reinterpret_cast<const phcu_program_t*>(s_prog);
+      const uint32_t step = blockDim.x;
       switch (T.vec) {
         case 4:
-          for (int64_t c = u0 + threadIdx.x; c < u1; c += blockDim.x) row_chunk<MAXIN, 4>(p, prog, (uint32_t)c, st);
+          for (int64_t c = u0 + threadIdx.x; c < u1; c += (int64_t)step * (E / 4))
+            row_group<S, MAXIN, 4, E / 4, true, false>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
           break;
         case 2:
-          for (int64_t c = u0 + threadIdx.x; c < u1; c += blockDim.x) row_chunk<MAXIN, 2>(p, prog, (uint32_t)c, st);
+          for (int64_t c = u0 + threadIdx.x; c < u1; c += (int64_t)step * (E / 2))
+            row_group<S, MAXIN, 2, E / 2, true, false>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
           break;
         default:
-          for (int64_t c = u0 + threadIdx.x; c < u1; c += blockDim.x) row_chunk<MAXIN, 1>(p, prog, (uint32_t)c, st);
+          for (int64_t c = u0 + threadIdx.x; c < u1; c += (int64_t)step * E)
+            row_group<S, MAXIN, 1, E, true, false>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
       }
     } else if (kind == BK_TILE) {
       const EvalPlan& p = *reinterpret_cast<const EvalPlan*>(s_plan);
       const phcu_program_t& prog = *reinterpret_cast<const phcu_program_t*>(s_prog);
-      for (int64_t t = u0; t < u1; t++) tile_body<MAXIN>(p, prog, (uint64_t)t, tiles, st);
+      for (int64_t t = u0; t < u1; t++) tile_body<S, MAXIN, true, false>(p, prog, (uint64_t)t, tiles, st);
     } else {
       const RedArgs& a = *reinterpret_cast<const RedArgs*>(s_plan);
       dispatch_reduce(a, T.rmode, u0, u1, st);
@@ -211,6 +218,8 @@ struct Batch {
   int32_t n_counters = 0;
   int64_t bytes = 0;
   size_t smem = 0;
+  int max_staged = 0;
+  bool narrow = true;  // every program fits 32-bit slots
   int grid = 0;
   cudaGraphExec_t graph = nullptr;
   cudaStream_t graph_stream = nullptr;
@@ -289,11 +298,12 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
       if (bt.ep.mode == MODE_EMPTY) continue;
       bt.prog = t.prog;
       bt.bytes = eval_bytes(bt.ep);
+      if (!program_is_32bit(programs[t.prog], bt.ep)) b->narrow = false;
       if (bt.ep.mode == MODE_TILE) {
         bt.kind = BK_TILE;
         bt.nunits = bt.ep.tiles_w * bt.ep.tiles_r * bt.ep.nbatch;
         bt.per_item = std::max<int64_t>(1, chunk / (TILE * TILE));
-        b->smem = std::max(b->smem, tile_smem_bytes(bt.ep.staged));
+        b->max_staged = std::max(b->max_staged, __builtin_popcount(bt.ep.staged));
       } else {
         bt.kind = BK_ROW;
         bt.vec = bt.ep.vec;
@@ -322,6 +332,7 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
         bt.nunits = bt.ep.sp.n / bt.ep.vec;
         bt.per_item = std::max<int64_t>(1, chunk / bt.ep.vec);
         bt.bytes = bt.ep.sp.n * dtype_size(t.out.dtype);
+        if (dtype_size(t.out.dtype) == 8) b->narrow = false;
       } else {
         bt.kind = BK_REDUCE;
         bt.rG = sh.G;
@@ -394,9 +405,17 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
     free_batch(b);
     return cuda_fail(e, "batch upload");
   }
-  if (b->smem > 48 * 1024) cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+  b->smem = (size_t)b->max_staged * TILE * (TILE + 1) * (b->narrow ? 4 : 8);
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, BATCH_THREADS, b->smem);
+  if (b->narrow) {
+    if (b->smem > 48 * 1024)
+      cudaFuncSetAttribute(batch_kernel<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<uint32_t>, BATCH_THREADS, b->smem);
+  } else {
+    if (b->smem > 48 * 1024)
+      cudaFuncSetAttribute(batch_kernel<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<uint64_t>, BATCH_THREADS, b->smem);
+  }
   if (per_sm < 1) per_sm = 1;
   b->grid = ctx().sm_count * per_sm;
   *out = b;
@@ -420,7 +439,8 @@ int32_t batch_launch(Batch* b, int mode) {
     A.n_items = b->n_items;
     A.deadline_ns = 20ull * 1000 * 1000 * 1000;  // 20 s
     int grid = (int)std::min<int64_t>(b->grid, b->n_items);
-    batch_kernel<<<grid, BATCH_THREADS, b->smem, s>>>(A);
+    if (b->narrow) batch_kernel<uint32_t><<<grid, BATCH_THREADS, b->smem, s>>>(A);
+    else batch_kernel<uint64_t><<<grid, BATCH_THREADS, b->smem, s>>>(A);
     count_launch();
     return check_launch("batch_kernel");
   }

@@ -1,92 +1,32 @@
-// eval.cu -- strided gather/scatter and fused elementwise kernels.
+// eval.cu -- strided gather/scatter and fused elementwise entry points.
 //
 // One kernel family serves copies (the empty program), fills (no inputs),
 // single infix operators and whole fused chains.  Two launch shapes:
 //
 //  ROW  -- the output and every input share the innermost canonical axis.
-//          Each thread handles VEC consecutive elements of one row; operands
-//          with unit (or reversed unit) inner stride use 128-bit accesses.
+//          Each thread handles several chunks of VEC consecutive elements;
+//          operands with unit (or reversed unit) inner stride use 128-bit
+//          accesses.
 //  TILE -- the output is contiguous along axis W while (some) inputs are
 //          contiguous along another axis R (permuted views).  A 64x64 tile of
 //          each such input is read coalesced along R into shared memory, then
 //          read back transposed so the output is written coalesced along W.
-#include "eval_device.cuh"
+// Kernels are instantiated in eval_inst_*.cu; this file plans and dispatches.
+#include "eval_kernels.cuh"
 
 namespace phcu {
 
-struct EvalArgs {
-  EvalPlan plan;
-  phcu_program_t prog;
-  uint32_t* status;
-};
-
-constexpr int ROW_THREADS = 256;
-
-template <int NIN, int VEC>
-__global__ void __launch_bounds__(ROW_THREADS) eval_row_kernel(const __grid_constant__ EvalArgs A) {
-  const uint32_t nchunks = (uint32_t)(A.plan.sp.n / VEC);
-  uint32_t st = 0;
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nchunks; c += gridDim.x * blockDim.x)
-    row_chunk<NIN, VEC>(A.plan, A.prog, c, st);
-  if (st) report_status(A.status, st);
-}
-
-template <int NIN>
-__global__ void __launch_bounds__(TILE_THREADS) eval_tile_kernel(const __grid_constant__ EvalArgs A) {
-  extern __shared__ uint64_t smem[];
-  uint32_t st = 0;
-  const uint64_t ntiles = (uint64_t)A.plan.tiles_w * A.plan.tiles_r * A.plan.nbatch;
-  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) tile_body<NIN>(A.plan, A.prog, t, smem, st);
-  if (st) report_status(A.status, st);
-}
-
-// ----------------------------------------------------------- dispatch
-template <int NIN>
-static int32_t launch_nin(const EvalArgs& A) {
-  const EvalPlan& p = A.plan;
-  Context& c = ctx();
-  if (p.mode == MODE_TILE) {
-    int nstaged = __builtin_popcount(p.staged);
-    size_t smem = (size_t)nstaged * TILE * (TILE + 1) * sizeof(uint64_t);
-    if (smem > 48 * 1024) {
-      cudaFuncSetAttribute(eval_tile_kernel<NIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    }
-    uint64_t ntiles = (uint64_t)p.tiles_w * p.tiles_r * p.nbatch;
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eval_tile_kernel<NIN>, TILE_THREADS, smem);
-    if (per_sm < 1) per_sm = 1;
-    uint64_t grid = (uint64_t)c.sm_count * per_sm;
-    if (grid > ntiles) grid = ntiles;
-    eval_tile_kernel<NIN><<<(unsigned)grid, TILE_THREADS, smem, c.stream>>>(A);
-    count_launch();
-    return check_launch("eval_tile_kernel");
-  }
-  // ROW
-  uint64_t nchunks = (uint64_t)p.sp.n / p.vec;
-  uint64_t blocks = (nchunks + ROW_THREADS - 1) / ROW_THREADS;
-  uint64_t cap = (uint64_t)c.sm_count * (2048 / ROW_THREADS) * 4;
-  if (blocks > cap) blocks = cap;
-  if (blocks == 0) blocks = 1;
-  switch (p.vec) {
-    case 4: eval_row_kernel<NIN, 4><<<(unsigned)blocks, ROW_THREADS, 0, c.stream>>>(A); break;
-    case 2: eval_row_kernel<NIN, 2><<<(unsigned)blocks, ROW_THREADS, 0, c.stream>>>(A); break;
-    default: eval_row_kernel<NIN, 1><<<(unsigned)blocks, ROW_THREADS, 0, c.stream>>>(A); break;
-  }
-  count_launch();
-  return check_launch("eval_row_kernel");
-}
+int32_t launch_eval_u32_lo(const EvalArgs& A);
+int32_t launch_eval_u32_hi(const EvalArgs& A);
+int32_t launch_eval_u64_lo(const EvalArgs& A);
+int32_t launch_eval_u64_hi(const EvalArgs& A);
 
 int32_t launch_eval(const EvalArgs& A) {
-  switch (A.plan.nin) {
-    case 0: return launch_nin<0>(A);
-    case 1: return launch_nin<1>(A);
-    case 2: return launch_nin<2>(A);
-    case 3: return launch_nin<3>(A);
-    case 4: return launch_nin<4>(A);
-  }
-  return fail(PHCU_ERR_INVALID, "too many inputs (%d > %d)", A.plan.nin, MAXIN);
+  if (A.plan.nin < 0 || A.plan.nin > MAXIN) return fail(PHCU_ERR_INVALID, "too many inputs (%d)", A.plan.nin);
+  const bool narrow = program_is_32bit(A.prog, A.plan);
+  if (narrow) return A.plan.nin <= 2 ? launch_eval_u32_lo(A) : launch_eval_u32_hi(A);
+  return A.plan.nin <= 2 ? launch_eval_u64_lo(A) : launch_eval_u64_hi(A);
 }
-
 // Launches an already planned operation (used by the batched executor's per-op replay).
 int32_t launch_eval_plan(const EvalPlan& plan, const phcu_program_t& prog) {
   EvalArgs A;

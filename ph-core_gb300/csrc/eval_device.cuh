@@ -1,6 +1,11 @@
-// eval_device.cuh -- per-chunk and per-tile bodies of the elementwise kernels,
-// shared by the standalone launches (eval.cu) and the persistent batched
-// executor (batch.cu).
+// eval_device.cuh -- bodies of the elementwise kernels (gather, scatter, fill,
+// infix operators, fused chains), shared by the standalone launches (eval.cu)
+// and the persistent batched executor (batch.cu).
+//
+// Memory-level parallelism is the design goal: every thread issues all loads
+// of U row chunks (ROW) or of its 16 tile elements (TILE) before it consumes
+// any of them, and the element-type switches sit outside the element loops so
+// the loads are straight-line code.
 #pragma once
 
 #include "plan.h"
@@ -8,57 +13,171 @@
 
 namespace phcu {
 
-// ROW: VEC consecutive elements (chunk c) of the canonical space.  Inputs k with
-// k >= p.nin are skipped, so an NIN=4 instantiation serves any input count.
-template <int NIN, int VEC>
-__device__ __forceinline__ void row_chunk(const EvalPlan& p, const phcu_program_t& prog, uint32_t c, uint32_t& st) {
-  const int W = p.sp.rank - 1;
-  const uint32_t e0 = c * VEC;
-  uint32_t row, col;
-  p.lendiv.divmod(e0, row, col);
-  int64_t off_out = (int64_t)col * p.out.stride[W];
-  int64_t off_in[NIN > 0 ? NIN : 1];
-#pragma unroll
-  for (int k = 0; k < NIN; k++) off_in[k] = (int64_t)col * p.in[k].stride[W];
-  uint32_t r = row;
-  for (int a = W - 1; a >= 0; a--) {
-    uint32_t q, x;
-    p.sp.div[a].divmod(r, q, x);
-    r = q;
-    off_out += (int64_t)x * p.out.stride[a];
-#pragma unroll
-    for (int k = 0; k < NIN; k++) off_in[k] += (int64_t)x * p.in[k].stride[a];
-  }
-  uint64_t in[NIN > 0 ? NIN : 1][VEC];
-#pragma unroll
-  for (int k = 0; k < NIN; k++) {
-    if (k < p.nin) {
-      const int es = dtype_size(p.in[k].dtype);
-      load_operand<VEC>(p.in[k].base + off_in[k] * es, p.in[k].stride[W], p.in[k].dtype, p.in[k].vmode, in[k]);
-    } else {
-#pragma unroll
-      for (int v = 0; v < VEC; v++) in[k][v] = 0;
-    }
-  }
-  uint64_t acc[VEC];
-  run_program<NIN, VEC>(prog, in, acc, st);
-  const int oes = dtype_size(p.out.dtype);
-  char* op = (char*)p.out.base + off_out * oes;
-  if (p.out.vmode == VM_VEC) store_vec<VEC>(op, p.out.dtype, acc);
-  else store_scalar<VEC>(op, p.out.stride[W] * oes, p.out.dtype, acc);
-}
-
 constexpr int TILE_THREADS = 256;
 
-// TILE: one TILE x TILE tile t (all threads of the block take part; contains
-// __syncthreads).  smem holds one TILE x (TILE+1) slot array per staged input.
-template <int NIN>
-__device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_t& prog, uint64_t t, uint64_t* smem,
+// ----------------------------------------------------------------- ROW
+// U chunks of VEC consecutive elements: chunk u is c0 + u * cstep.
+template <typename S, int NIN, int VEC, int U, bool STASH, bool COPY>
+__device__ __forceinline__ void row_group(const EvalPlan& p, const phcu_program_t& prog, uint32_t c0, uint32_t cstep,
+                                          uint32_t nchunks, uint32_t& st) {
+  constexpr int V = VEC * U;
+  const int W = p.sp.rank - 1;
+  int64_t off_out[U];
+  int64_t off_in[NIN > 0 ? NIN : 1][U];
+  bool valid[U];
+#pragma unroll
+  for (int u = 0; u < U; u++) {
+    // a chunk past the end repeats chunk c0 (always valid): its values are
+    // computed but not stored, so they raise no spurious status bits
+    uint32_t c = c0 + (uint32_t)u * cstep;
+    valid[u] = c < nchunks;
+    if (!valid[u]) c = c0;
+    uint32_t row, col;
+    p.lendiv.divmod(c * VEC, row, col);
+    off_out[u] = (int64_t)col * p.out.stride[W];
+#pragma unroll
+    for (int k = 0; k < NIN; k++) off_in[k][u] = (int64_t)col * p.in[k].stride[W];
+    for (int a = W - 1; a >= 0; a--) {
+      uint32_t q, x;
+      p.sp.div[a].divmod(row, q, x);
+      row = q;
+      off_out[u] += (int64_t)x * p.out.stride[a];
+#pragma unroll
+      for (int k = 0; k < NIN; k++) off_in[k][u] += (int64_t)x * p.in[k].stride[a];
+    }
+  }
+  S in[NIN > 0 ? NIN : 1][V];
+#pragma unroll
+  for (int k = 0; k < NIN; k++) {
+    if (k >= p.nin) continue;
+    const char* base = p.in[k].base;
+    const int64_t sw = p.in[k].stride[W];
+    const int vm = p.in[k].vmode;
+    switch (dtype_size(p.in[k].dtype)) {
+      case 4:
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          ld_operand<S, 4, VEC>(base + off_in[k][u] * 4, sw, vm, &in[k][u * VEC]);
+        break;
+      case 8:
+        if constexpr (sizeof(S) == 8) {
+#pragma unroll
+          for (int u = 0; u < U; u++)
+            ld_operand<S, 8, VEC>(base + off_in[k][u] * 8, sw, vm, &in[k][u * VEC]);
+        }
+        break;
+      default:
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          ld_operand<S, 1, VEC>(base + off_in[k][u], sw, vm, &in[k][u * VEC]);
+    }
+  }
+  S acc[V];
+  if constexpr (COPY) {
+#pragma unroll
+    for (int v = 0; v < V; v++) acc[v] = in[0][v];
+  } else {
+    run_program<S, NIN, V, STASH>(prog, in, acc, st);
+  }
+  char* obase = (char*)p.out.base;
+  const int64_t so = p.out.stride[W];
+  const int om = p.out.vmode;
+  switch (dtype_size(p.out.dtype)) {
+    case 4:
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (valid[u]) st_operand<S, 4, VEC>(obase + off_out[u] * 4, so, om, &acc[u * VEC]);
+      break;
+    case 8:
+      if constexpr (sizeof(S) == 8) {
+#pragma unroll
+        for (int u = 0; u < U; u++)
+          if (valid[u]) st_operand<S, 8, VEC>(obase + off_out[u] * 8, so, om, &acc[u * VEC]);
+      }
+      break;
+    default:
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        if (valid[u]) st_operand<S, 1, VEC>(obase + off_out[u], so, om, &acc[u * VEC]);
+  }
+}
+
+// ----------------------------------------------------------------- TILE
+// Loads this thread's 16 elements of a TILE x TILE block of one staged input
+// (coalesced along R) and writes them to the shared tile.
+template <typename S, int ES>
+__device__ __forceinline__ void stage_tile(const char* base, int64_t sr, int64_t sw, int64_t nr, int64_t nw, S* tile) {
+  constexpr int LD = TILE + 1;
+  constexpr int NWARP = TILE_THREADS / 32;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  // coordinates past the edge of a partial tile repeat the last valid element,
+  // so every value the program sees is a real element (no spurious status bits)
+  S v[TILE / NWARP][TILE / 32];
+#pragma unroll
+  for (int i = 0; i < TILE / NWARP; i++) {
+    const int64_t w = min((int64_t)(warp + i * NWARP), nw - 1);
+#pragma unroll
+    for (int j = 0; j < TILE / 32; j++) {
+      const int64_t r = min((int64_t)(lane + 32 * j), nr - 1);
+      v[i][j] = ld_elem<S, ES>(base + (r * sr + w * sw) * ES);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < TILE / NWARP; i++) {
+    const int w = warp + i * NWARP;
+#pragma unroll
+    for (int j = 0; j < TILE / 32; j++) tile[w * LD + lane + 32 * j] = v[i][j];
+  }
+}
+
+// Elements handled by one thread in phase 2: rows r = warp + NWARP*i (i < NI),
+// columns w = lane + 32*j (j < TILE/32), i.e. NI*2 elements per pass.
+template <typename S, int ES, int NI>
+__device__ __forceinline__ void tile_direct_load(const char* base, int64_t sr, int64_t sw, int r_first, int64_t nr,
+                                                 int64_t nw, S* out) {
+  constexpr int NWARP = TILE_THREADS / 32;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NI; i++) {
+    const int64_t r = min((int64_t)(r_first + warp + NWARP * i), nr - 1);
+#pragma unroll
+    for (int j = 0; j < TILE / 32; j++) {
+      const int64_t w = min((int64_t)(lane + 32 * j), nw - 1);
+      out[i * (TILE / 32) + j] = ld_elem<S, ES>(base + (r * sr + w * sw) * ES);
+    }
+  }
+}
+
+template <typename S, int ES, int NI>
+__device__ __forceinline__ void tile_store(char* obase, int64_t so_r, int r_first, int64_t nr, int64_t nw,
+                                           const S* acc) {
+  constexpr int NWARP = TILE_THREADS / 32;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NI; i++) {
+    const int r = r_first + warp + NWARP * i;
+#pragma unroll
+    for (int j = 0; j < TILE / 32; j++) {
+      const int w = lane + 32 * j;
+      if (r < nr && w < nw) st_elem<S, ES>(obase + ((int64_t)r * so_r + w) * ES, acc[i * (TILE / 32) + j]);
+    }
+  }
+}
+
+// One TILE x TILE tile t (every thread of the block takes part; contains
+// __syncthreads).  smem holds one TILE x (TILE+1) array of S per staged input.
+template <typename S, int NIN, bool STASH, bool COPY>
+__device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_t& prog, uint64_t t, S* smem,
                                           uint32_t& st) {
   const int W = p.sp.rank - 1;
   const int R = p.raxis;
   constexpr int LD = TILE + 1;
   constexpr int NWARP = TILE_THREADS / 32;
+  constexpr int NI = (sizeof(S) == 4) ? TILE / NWARP : TILE / NWARP / 2;  // rows per pass
+  constexpr int V = NI * (TILE / 32);
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   uint32_t rest, tw, tr, b;
@@ -87,67 +206,112 @@ __device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_
 #pragma unroll
   for (int k = 0; k < NIN; k++) {
     if (k >= p.nin || !(p.staged & (1u << k))) continue;
-    uint64_t* tile = smem + (size_t)slot * TILE * LD;
+    S* tile = smem + (size_t)slot * TILE * LD;
     slot++;
-    const int es = dtype_size(p.in[k].dtype);
     const int64_t sr = p.in[k].stride[R], sw = p.in[k].stride[W];
-    const char* base = p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * es;
-#pragma unroll
-    for (int i = 0; i < TILE / NWARP; i++) {
-      const int w = warp + i * NWARP;
-#pragma unroll
-      for (int j = 0; j < TILE / 32; j++) {
-        const int r = lane + 32 * j;
-        if (w < nw && r < nr) {
-          uint64_t v[1];
-          load_scalar<1>(base + ((int64_t)r * sr + (int64_t)w * sw) * es, 0, p.in[k].dtype, v);
-          tile[w * LD + r] = v[0];
-        }
-      }
+    switch (dtype_size(p.in[k].dtype)) {
+      case 4: stage_tile<S, 4>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 4, sr, sw, nr, nw, tile); break;
+      case 8:
+        if constexpr (sizeof(S) == 8)
+          stage_tile<S, 8>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 8, sr, sw, nr, nw, tile);
+        break;
+      default: stage_tile<S, 1>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw), sr, sw, nr, nw, tile);
     }
   }
-  if (p.staged) __syncthreads();
+  __syncthreads();
 
-  // phase 2: compute and write coalesced along W
+  // phase 2: compute and write coalesced along W, V elements per pass
+  char* obase = (char*)p.out.base;
+  const int64_t so_r = p.out.stride[R];
   const int oes = dtype_size(p.out.dtype);
-  char* obase = (char*)p.out.base + (off_out + r0 * p.out.stride[R] + w0) * oes;
-#pragma unroll 4
-  for (int i = 0; i < TILE / NWARP; i++) {
-    const int r = warp + i * NWARP;
+  obase += (off_out + r0 * so_r + w0) * oes;
+#pragma unroll 1
+  for (int pass = 0; pass < (TILE / NWARP) / NI; pass++) {
+    const int r_first = pass * NI * NWARP;
+    S in[NIN > 0 ? NIN : 1][V];
+    int s2 = 0;
 #pragma unroll
-    for (int j = 0; j < TILE / 32; j++) {
-      const int w = lane + 32 * j;
-      if (r < nr && w < nw) {
-        uint64_t in[NIN > 0 ? NIN : 1][1];
-        int s2 = 0;
+    for (int k = 0; k < NIN; k++) {
+      if (k >= p.nin) continue;
+      if (p.staged & (1u << k)) {
+        const S* tile = smem + (size_t)s2 * TILE * LD;
+        s2++;
 #pragma unroll
-        for (int k = 0; k < NIN; k++) {
-          if (k >= p.nin) {
-            in[k][0] = 0;
-          } else if (p.staged & (1u << k)) {
-            in[k][0] = smem[(size_t)s2 * TILE * LD + w * LD + r];
-            s2++;
-          } else {
-            const int es = dtype_size(p.in[k].dtype);
-            uint64_t v[1];
-            load_scalar<1>(p.in[k].base +
-                               (off_in[k] + (r0 + r) * p.in[k].stride[R] + (w0 + w) * p.in[k].stride[W]) * es,
-                           0, p.in[k].dtype, v);
-            in[k][0] = v[0];
-          }
+        for (int i = 0; i < NI; i++) {
+#pragma unroll
+          for (int j = 0; j < TILE / 32; j++)
+            in[k][i * (TILE / 32) + j] = tile[(lane + 32 * j) * LD + r_first + warp + NWARP * i];
         }
-        uint64_t acc[1];
-        run_program<NIN, 1>(prog, in, acc, st);
-        uint64_t o[1] = {acc[0]};
-        store_scalar<1>(obase + ((int64_t)r * p.out.stride[R] + w) * oes, 0, p.out.dtype, o);
+      } else {
+        const int64_t sr = p.in[k].stride[R], sw = p.in[k].stride[W];
+        switch (dtype_size(p.in[k].dtype)) {
+          case 4:
+            tile_direct_load<S, 4, NI>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 4, sr, sw, r_first, nr, nw,
+                                       in[k]);
+            break;
+          case 8:
+            if constexpr (sizeof(S) == 8)
+              tile_direct_load<S, 8, NI>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 8, sr, sw, r_first, nr,
+                                         nw, in[k]);
+            break;
+          default:
+            tile_direct_load<S, 1, NI>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw), sr, sw, r_first, nr, nw,
+                                       in[k]);
+        }
       }
     }
+    S acc[V];
+    if constexpr (COPY) {
+#pragma unroll
+      for (int v = 0; v < V; v++) acc[v] = in[0][v];
+    } else {
+      run_program<S, NIN, V, STASH>(prog, in, acc, st);
+    }
+    switch (oes) {
+      case 4: tile_store<S, 4, NI>(obase, so_r, r_first, nr, nw, acc); break;
+      case 8:
+        if constexpr (sizeof(S) == 8) tile_store<S, 8, NI>(obase, so_r, r_first, nr, nw, acc);
+        break;
+      default: tile_store<S, 1, NI>(obase, so_r, r_first, nr, nw, acc);
+    }
   }
-  if (p.staged) __syncthreads();
+  __syncthreads();
 }
 
+template <typename S>
 inline size_t tile_smem_bytes(uint32_t staged) {
-  return (size_t)__builtin_popcount(staged) * TILE * (TILE + 1) * sizeof(uint64_t);
+  return (size_t)__builtin_popcount(staged) * TILE * (TILE + 1) * sizeof(S);
+}
+
+// ------------------------------------------------------- program traits
+// Whether every value the program (and its operands) touches fits 32 bits.
+inline bool program_is_32bit(const phcu_program_t& P, const EvalPlan& plan) {
+  auto wide = [](int t) { return t == PHCU_I64 || t == PHCU_F64; };
+  if (wide(P.out_type) || wide(plan.out.dtype)) return false;
+  for (int k = 0; k < plan.nin; k++)
+    if (wide(plan.in[k].dtype)) return false;
+  for (int i = 0; i < P.n_instr; i++) {
+    const phcu_instr_t& I = P.code[i];
+    if (wide(I.type) || wide(I.btype)) return false;
+    if (I.op == PHCU_I_CVT && wide((int)I.imm.i)) return false;
+    if (I.op == PHCU_OP_DIV && is_int_t(I.type)) return false;  // Int / Int -> Float64
+  }
+  return true;
+}
+
+inline bool program_uses_stash(const phcu_program_t& P) {
+  for (int i = 0; i < P.n_instr; i++) {
+    const phcu_instr_t& I = P.code[i];
+    if (I.op == PHCU_I_ST0 || I.op == PHCU_I_ST1) return true;
+  }
+  return false;
+}
+
+// A plain move: one input, one LD of its own type into an output of that type.
+inline bool program_is_copy(const phcu_program_t& P, const EvalPlan& plan) {
+  return plan.nin == 1 && P.n_instr == 1 && P.code[0].op == PHCU_I_LD && P.code[0].src == 0 &&
+         P.code[0].type == P.code[0].btype && P.code[0].type == plan.in[0].dtype && P.out_type == plan.out.dtype &&
+         plan.in[0].dtype == plan.out.dtype;
 }
 
 }  // namespace phcu

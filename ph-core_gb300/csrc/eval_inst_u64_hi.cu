@@ -1,0 +1,15 @@
+// eval_inst_u64_hi.cu -- instantiations of the elementwise kernels with
+// uint64_t slots for the 3-4-input programs (split for parallel compilation).
+#include "eval_kernels.cuh"
+
+namespace phcu {
+
+int32_t launch_eval_u64_hi(const EvalArgs& A) {
+  switch (A.plan.nin) {
+    case 3: return launch_eval_sn<uint64_t, 3>(A);
+    case 4: return launch_eval_sn<uint64_t, 4>(A);
+  }
+  return fail(PHCU_ERR_INVALID, "input count %d not handled here", A.plan.nin);
+}
+
+}  // namespace phcu

@@ -1,0 +1,102 @@
+// eval_kernels.cuh -- the standalone ROW and TILE kernels and their launcher,
+// instantiated per (slot type, input count) in eval_inst_*.cu so the
+// translation units compile in parallel.
+#pragma once
+
+#include "eval_device.cuh"
+
+namespace phcu {
+
+struct EvalArgs {
+  EvalPlan plan;
+  phcu_program_t prog;
+  uint32_t* status;
+};
+
+constexpr int ROW_THREADS = 256;
+
+// ROW: each thread handles U grid-strided chunks of VEC elements per iteration
+// (16 elements with 32-bit slots, 8 with 64-bit slots).
+template <typename S, int NIN, int VEC, int U, bool STASH, bool COPY>
+__global__ void __launch_bounds__(ROW_THREADS) eval_row_kernel(const __grid_constant__ EvalArgs A) {
+  const uint32_t nchunks = (uint32_t)(A.plan.sp.n / VEC);
+  const uint32_t nthreads = gridDim.x * blockDim.x;
+  uint32_t st = 0;
+  for (uint32_t c0 = blockIdx.x * blockDim.x + threadIdx.x; c0 < nchunks; c0 += nthreads * U)
+    row_group<S, NIN, VEC, U, STASH, COPY>(A.plan, A.prog, c0, nthreads, nchunks, st);
+  if (st) report_status(A.status, st);
+}
+
+template <typename S, int NIN, bool STASH, bool COPY>
+__global__ void __launch_bounds__(TILE_THREADS) eval_tile_kernel(const __grid_constant__ EvalArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  S* smem = reinterpret_cast<S*>(smem_raw);
+  uint32_t st = 0;
+  const uint64_t ntiles = (uint64_t)A.plan.tiles_w * A.plan.tiles_r * A.plan.nbatch;
+  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) tile_body<S, NIN, STASH, COPY>(A.plan, A.prog, t, smem, st);
+  if (st) report_status(A.status, st);
+}
+
+template <typename K>
+static int32_t launch_grid(K kernel, const EvalArgs& A, uint64_t work_blocks, int threads, size_t smem,
+                           const char* what) {
+  Context& c = ctx();
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  if (per_sm < 1) per_sm = 1;
+  uint64_t grid = (uint64_t)c.sm_count * per_sm;
+  if (grid > work_blocks) grid = work_blocks;
+  if (grid < 1) grid = 1;
+  kernel<<<(unsigned)grid, threads, smem, c.stream>>>(A);
+  count_launch();
+  return check_launch(what);
+}
+
+template <typename S, int NIN, bool STASH, bool COPY>
+static int32_t launch_row(const EvalArgs& A) {
+  constexpr int E = sizeof(S) == 4 ? 16 : 8;  // elements per thread per iteration
+  const uint64_t n = (uint64_t)A.plan.sp.n;
+  switch (A.plan.vec) {
+    case 4: {
+      const uint64_t wb = (n / 4 + ROW_THREADS * (E / 4) - 1) / (ROW_THREADS * (E / 4));
+      return launch_grid(eval_row_kernel<S, NIN, 4, E / 4, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
+    }
+    case 2: {
+      const uint64_t wb = (n / 2 + ROW_THREADS * (E / 2) - 1) / (ROW_THREADS * (E / 2));
+      return launch_grid(eval_row_kernel<S, NIN, 2, E / 2, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
+    }
+    default: {
+      const uint64_t wb = (n + ROW_THREADS * E - 1) / (ROW_THREADS * E);
+      return launch_grid(eval_row_kernel<S, NIN, 1, E, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
+    }
+  }
+}
+
+template <typename S, int NIN, bool STASH, bool COPY>
+static int32_t launch_tile(const EvalArgs& A) {
+  const size_t smem = tile_smem_bytes<S>(A.plan.staged);
+  const uint64_t ntiles = (uint64_t)A.plan.tiles_w * A.plan.tiles_r * A.plan.nbatch;
+  return launch_grid(eval_tile_kernel<S, NIN, STASH, COPY>, A, ntiles, TILE_THREADS, smem, "eval_tile_kernel");
+}
+
+template <typename S, int NIN>
+int32_t launch_eval_sn(const EvalArgs& A) {
+  const bool stash = program_uses_stash(A.prog);
+  if (A.plan.mode == MODE_TILE) {
+    if constexpr (NIN == 1) {
+      if (program_is_copy(A.prog, A.plan)) return launch_tile<S, NIN, false, true>(A);
+    }
+    return stash ? launch_tile<S, NIN, true, false>(A) : launch_tile<S, NIN, false, false>(A);
+  }
+  if constexpr (NIN == 1) {
+    if (program_is_copy(A.prog, A.plan)) return launch_row<S, NIN, false, true>(A);
+  }
+  return stash ? launch_row<S, NIN, true, false>(A) : launch_row<S, NIN, false, false>(A);
+}
+
+// defined in eval_inst_*.cu
+int32_t launch_eval_u32(const EvalArgs& A);
+int32_t launch_eval_u64(const EvalArgs& A);
+
+}  // namespace phcu

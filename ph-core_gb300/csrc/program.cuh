@@ -1,49 +1,56 @@
 // program.cuh -- the fixed-opcode accumulator machine evaluated per element.
 //
-// Values live in 64-bit slots: Float32 and Int32 in the low 32 bits, Int64 and
-// Float64 in all 64, Bool as 0/1.  Every instruction is uniform across the
-// grid, so the switches below are uniform branches; each thread applies an
-// instruction to VEC elements held in registers.  Semantics follow Crystal 1.0
-// numbers (checked Int32/Int64 + - *, floor division and modulo, Int / Int ->
-// Float64, Float ** Int by binary exponentiation), matching the CPU oracle.
-// This translation unit is compiled with -fmad=false: no FMA contraction, so
-// every Float32 operation rounds once, as on the host.
+// Values live in slots of type S: uint32_t when every type the program
+// touches is 32-bit or narrower (Float32, Int32, Bool), uint64_t otherwise.
+// Float32 and Int32 occupy the low 32 bits, Int64 and Float64 all 64, Bool is
+// 0/1.  Every instruction is uniform across the grid, so each instruction is
+// dispatched ONCE per thread (uniform branches) and then applied to the V
+// elements the thread holds in registers; per element only the arithmetic
+// itself runs.  Semantics follow Crystal 1.0 numbers (checked Int32/Int64
+// + - *, floor division and modulo, Int / Int -> Float64, Float ** Int by
+// binary exponentiation), matching the CPU oracle.  Translation units that
+// include this file are compiled with -fmad=false: every Float32 operation
+// rounds once, as on the host.
 #pragma once
+
+#include <type_traits>
 
 #include "common.cuh"
 
 namespace phcu {
 
-__device__ __forceinline__ float sf32(uint64_t s) { return __uint_as_float((uint32_t)s); }
-__device__ __forceinline__ uint64_t pf32(float f) { return (uint64_t)__float_as_uint(f); }
+// ----------------------------------------------------------- slot access
+template <typename S>
+__device__ __forceinline__ float sf32(S s) { return __uint_as_float((uint32_t)s); }
+template <typename S>
+__device__ __forceinline__ S pf32(float f) { return (S)__float_as_uint(f); }
+template <typename S>
+__device__ __forceinline__ int32_t si32(S s) { return (int32_t)(uint32_t)s; }
+template <typename S>
+__device__ __forceinline__ S pi32(int32_t v) { return (S)(uint32_t)v; }
 __device__ __forceinline__ double sf64(uint64_t s) { return __longlong_as_double((long long)s); }
 __device__ __forceinline__ uint64_t pf64(double f) { return (uint64_t)__double_as_longlong(f); }
-__device__ __forceinline__ int32_t si32(uint64_t s) { return (int32_t)(uint32_t)s; }
-__device__ __forceinline__ uint64_t pi32(int32_t v) { return (uint64_t)(uint32_t)v; }
-__device__ __forceinline__ int64_t si64(uint64_t s) { return (int64_t)s; }
-__device__ __forceinline__ uint64_t pi64(int64_t v) { return (uint64_t)v; }
 
-// ---------------------------------------------------------------- loads
-template <int VEC>
-__device__ __forceinline__ void load_scalar(const char* p, int64_t stride_bytes, int dtype,
-                                            uint64_t (&v)[VEC]) {
-#pragma unroll
-  for (int i = 0; i < VEC; i++) {
-    const char* q = p + i * stride_bytes;
-    switch (dtype) {
-      case PHCU_BOOL: v[i] = (*(const uint8_t*)q) ? 1u : 0u; break;
-      case PHCU_I32:
-      case PHCU_F32: v[i] = (uint64_t)__ldg((const uint32_t*)q); break;
-      default: v[i] = (uint64_t)__ldg((const unsigned long long*)q); break;
-    }
-  }
+// ----------------------------------------------------------------- loads
+// One element of type dtype at p as a slot (the caller switches on dtype
+// outside its element loops).
+template <typename S, int ES>
+__device__ __forceinline__ S ld_elem(const char* p) {
+  if constexpr (ES == 4) return (S)__ldg((const uint32_t*)p);
+  else if constexpr (ES == 8) return (S)__ldg((const unsigned long long*)p);
+  else return (S)(*(const uint8_t*)p != 0);
+}
+template <typename S, int ES>
+__device__ __forceinline__ void st_elem(char* p, S v) {
+  if constexpr (ES == 4) *(uint32_t*)p = (uint32_t)v;
+  else if constexpr (ES == 8) *(unsigned long long*)p = (unsigned long long)v;
+  else *(uint8_t*)p = (uint8_t)(v & 1u);
 }
 
-// VEC consecutive elements starting at p (aligned to min(16, VEC*es) bytes).
-template <int VEC>
-__device__ __forceinline__ void load_vec(const char* p, int dtype, uint64_t (&v)[VEC]) {
-  const int es = dtype_size(dtype);
-  if (es == 4) {
+// VEC consecutive elements starting at p (aligned to min(16, VEC*ES) bytes).
+template <typename S, int ES, int VEC>
+__device__ __forceinline__ void ld_vec(const char* p, S* v) {
+  if constexpr (ES == 4) {
     if constexpr (VEC == 4) {
       uint4 x = __ldg((const uint4*)p);
       v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
@@ -53,50 +60,30 @@ __device__ __forceinline__ void load_vec(const char* p, int dtype, uint64_t (&v)
     } else {
       v[0] = __ldg((const uint32_t*)p);
     }
-  } else if (es == 8) {
+  } else if constexpr (ES == 8) {
     if constexpr (VEC == 4) {
       ulonglong2 x = __ldg((const ulonglong2*)p);
       ulonglong2 y = __ldg((const ulonglong2*)(p + 16));
-      v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
+      v[0] = (S)x.x; v[1] = (S)x.y; v[2] = (S)y.x; v[3] = (S)y.y;
     } else if constexpr (VEC == 2) {
       ulonglong2 x = __ldg((const ulonglong2*)p);
-      v[0] = x.x; v[1] = x.y;
+      v[0] = (S)x.x; v[1] = (S)x.y;
     } else {
-      v[0] = __ldg((const unsigned long long*)p);
+      v[0] = (S)__ldg((const unsigned long long*)p);
     }
-  } else {  // bool
+  } else {
 #pragma unroll
-    for (int i = 0; i < VEC; i++) v[i] = p[i] ? 1u : 0u;
+    for (int i = 0; i < VEC; i++) v[i] = (S)(p[i] != 0);
   }
 }
 
-template <int VEC>
-__device__ __forceinline__ void store_scalar(char* p, int64_t stride_bytes, int dtype,
-                                             const uint64_t (&v)[VEC]) {
-#pragma unroll
-  for (int i = 0; i < VEC; i++) {
-    char* q = p + i * stride_bytes;
-    switch (dtype) {
-      case PHCU_BOOL: *(uint8_t*)q = (uint8_t)(v[i] & 1u); break;
-      case PHCU_I32:
-      case PHCU_F32: *(uint32_t*)q = (uint32_t)v[i]; break;
-      default: *(unsigned long long*)q = (unsigned long long)v[i]; break;
-    }
-  }
-}
-
-template <int VEC>
-__device__ __forceinline__ void store_vec(char* p, int dtype, const uint64_t (&v)[VEC]) {
-  const int es = dtype_size(dtype);
-  if (es == 4) {
-    if constexpr (VEC == 4) {
-      *(uint4*)p = make_uint4((uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], (uint32_t)v[3]);
-    } else if constexpr (VEC == 2) {
-      *(uint2*)p = make_uint2((uint32_t)v[0], (uint32_t)v[1]);
-    } else {
-      *(uint32_t*)p = (uint32_t)v[0];
-    }
-  } else if (es == 8) {
+template <typename S, int ES, int VEC>
+__device__ __forceinline__ void st_vec(char* p, const S* v) {
+  if constexpr (ES == 4) {
+    if constexpr (VEC == 4) *(uint4*)p = make_uint4((uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], (uint32_t)v[3]);
+    else if constexpr (VEC == 2) *(uint2*)p = make_uint2((uint32_t)v[0], (uint32_t)v[1]);
+    else *(uint32_t*)p = (uint32_t)v[0];
+  } else if constexpr (ES == 8) {
     if constexpr (VEC == 4) {
       *(ulonglong2*)p = make_ulonglong2(v[0], v[1]);
       *(ulonglong2*)(p + 16) = make_ulonglong2(v[2], v[3]);
@@ -111,71 +98,91 @@ __device__ __forceinline__ void store_vec(char* p, int dtype, const uint64_t (&v
   }
 }
 
-// Loads VEC elements of one operand in the given vector mode.
-template <int VEC>
-__device__ __forceinline__ void load_operand(const char* p, int64_t inner_stride, int dtype, int vmode,
-                                             uint64_t (&v)[VEC]) {
-  const int es = dtype_size(dtype);
+// VEC elements of one operand in a vector mode: VM_VEC (unit stride),
+// VM_VEC_REV (stride -1, vector at the low end, reversed), VM_SCALAR.
+template <typename S, int ES, int VEC>
+__device__ __forceinline__ void ld_operand(const char* p, int64_t inner_stride, int vmode, S* v) {
   if (vmode == VM_VEC) {
-    load_vec<VEC>(p, dtype, v);
+    ld_vec<S, ES, VEC>(p, v);
   } else if (vmode == VM_VEC_REV) {
-    uint64_t t[VEC];
-    load_vec<VEC>(p - (VEC - 1) * es, dtype, t);
+    S t[VEC];
+    ld_vec<S, ES, VEC>(p - (VEC - 1) * ES, t);
 #pragma unroll
     for (int i = 0; i < VEC; i++) v[i] = t[VEC - 1 - i];
   } else {
-    load_scalar<VEC>(p, inner_stride * es, dtype, v);
+#pragma unroll
+    for (int i = 0; i < VEC; i++) v[i] = ld_elem<S, ES>(p + i * inner_stride * ES);
   }
 }
 
-// -------------------------------------------------------- conversions
-__device__ __forceinline__ uint64_t convert_slot(uint64_t s, int from, int to) {
-  if (from == to) return s;
-  switch (from) {
-    case PHCU_BOOL:
-    case PHCU_I32: {
-      int64_t x = (from == PHCU_BOOL) ? (int64_t)(s & 1u) : (int64_t)si32(s);
-      switch (to) {
-        case PHCU_I32: return pi32((int32_t)x);
-        case PHCU_I64: return pi64(x);
-        case PHCU_F32: return pf32((float)x);
-        case PHCU_F64: return pf64((double)x);
-        case PHCU_BOOL: return x != 0;
-      }
-      break;
-    }
-    case PHCU_I64: {
-      int64_t x = si64(s);
-      switch (to) {
-        case PHCU_I32: return pi32((int32_t)x);
-        case PHCU_F32: return pf32((float)x);
-        case PHCU_F64: return pf64((double)x);
-        case PHCU_BOOL: return x != 0;
-      }
-      break;
-    }
-    case PHCU_F32: {
-      float x = sf32(s);
-      switch (to) {
-        case PHCU_F64: return pf64((double)x);
-        case PHCU_I32: return pi32((int32_t)x);
-        case PHCU_I64: return pi64((int64_t)x);
-        case PHCU_BOOL: return x != 0.0f;
-      }
-      break;
-    }
-    case PHCU_F64: {
-      double x = sf64(s);
-      switch (to) {
-        case PHCU_F32: return pf32((float)x);
-        case PHCU_I32: return pi32((int32_t)x);
-        case PHCU_I64: return pi64((int64_t)x);
-        case PHCU_BOOL: return x != 0.0;
-      }
-      break;
-    }
+template <typename S, int ES, int VEC>
+__device__ __forceinline__ void st_operand(char* p, int64_t inner_stride, int vmode, const S* v) {
+  if (vmode == VM_VEC) {
+    st_vec<S, ES, VEC>(p, v);
+  } else {
+#pragma unroll
+    for (int i = 0; i < VEC; i++) st_elem<S, ES>(p + i * inner_stride * ES, v[i]);
   }
-  return s;
+}
+
+// ------------------------------------------------------- conversions
+template <typename S>
+__device__ __forceinline__ S convert_slot(S s, int from, int to) {
+  if (from == to) return s;
+  if constexpr (sizeof(S) == 4) {
+    switch (from) {
+      case PHCU_BOOL:
+      case PHCU_I32: {
+        int32_t x = (from == PHCU_BOOL) ? (int32_t)(s & 1u) : si32(s);
+        if (to == PHCU_F32) return pf32<S>((float)x);
+        if (to == PHCU_I32) return pi32<S>(x);
+        return (S)(x != 0);
+      }
+      case PHCU_F32: {
+        float x = sf32(s);
+        if (to == PHCU_I32) return pi32<S>((int32_t)x);
+        return (S)(x != 0.0f);
+      }
+    }
+    return s;
+  } else {
+    switch (from) {
+      case PHCU_BOOL:
+      case PHCU_I32:
+      case PHCU_I64: {
+        int64_t x = (from == PHCU_BOOL) ? (int64_t)(s & 1u) : (from == PHCU_I32) ? (int64_t)si32(s) : (int64_t)s;
+        switch (to) {
+          case PHCU_I32: return (S)(uint32_t)(int32_t)x;
+          case PHCU_I64: return (S)x;
+          case PHCU_F32: return pf32<S>((float)x);
+          case PHCU_F64: return pf64((double)x);
+          case PHCU_BOOL: return x != 0;
+        }
+        break;
+      }
+      case PHCU_F32: {
+        float x = sf32(s);
+        switch (to) {
+          case PHCU_F64: return pf64((double)x);
+          case PHCU_I32: return (S)(uint32_t)(int32_t)x;
+          case PHCU_I64: return (S)(int64_t)x;
+          case PHCU_BOOL: return x != 0.0f;
+        }
+        break;
+      }
+      case PHCU_F64: {
+        double x = sf64(s);
+        switch (to) {
+          case PHCU_F32: return pf32<S>((float)x);
+          case PHCU_I32: return (S)(uint32_t)(int32_t)x;
+          case PHCU_I64: return (S)(int64_t)x;
+          case PHCU_BOOL: return x != 0.0;
+        }
+        break;
+      }
+    }
+    return s;
+  }
 }
 
 // ------------------------------------------------------ integer helpers
@@ -189,22 +196,15 @@ __device__ __forceinline__ int64_t floormod_i64(int64_t a, int64_t b) {
   if (r != 0 && ((r < 0) != (b < 0))) r += b;
   return r;
 }
-
-template <typename I>
-__device__ __forceinline__ I wrap_mul(I a, I b) {
-  using U = typename std::conditional<sizeof(I) == 4, uint32_t, uint64_t>::type;
-  return (I)((U)a * (U)b);
-}
-
 __device__ __forceinline__ int32_t chk_add32(int32_t a, int32_t b, uint32_t& st) {
-  int64_t r = (int64_t)a + b;
-  if (r != (int32_t)r) st |= PHCU_ST_OVERFLOW;
-  return (int32_t)(uint32_t)(uint64_t)r;
+  int32_t r = (int32_t)((uint32_t)a + (uint32_t)b);
+  if (((a ^ r) & (b ^ r)) < 0) st |= PHCU_ST_OVERFLOW;
+  return r;
 }
 __device__ __forceinline__ int32_t chk_sub32(int32_t a, int32_t b, uint32_t& st) {
-  int64_t r = (int64_t)a - b;
-  if (r != (int32_t)r) st |= PHCU_ST_OVERFLOW;
-  return (int32_t)(uint32_t)(uint64_t)r;
+  int32_t r = (int32_t)((uint32_t)a - (uint32_t)b);
+  if (((a ^ b) & (a ^ r)) < 0) st |= PHCU_ST_OVERFLOW;
+  return r;
 }
 __device__ __forceinline__ int32_t chk_mul32(int32_t a, int32_t b, uint32_t& st) {
   int64_t r = (int64_t)a * b;
@@ -223,9 +223,13 @@ __device__ __forceinline__ int64_t chk_sub64(int64_t a, int64_t b, uint32_t& st)
 }
 __device__ __forceinline__ int64_t chk_mul64(int64_t a, int64_t b, uint32_t& st) {
   int64_t r = (int64_t)((uint64_t)a * (uint64_t)b);
-  int64_t hi = __mul64hi(a, b);
-  if (hi != (r >> 63)) st |= PHCU_ST_OVERFLOW;
+  if (__mul64hi(a, b) != (r >> 63)) st |= PHCU_ST_OVERFLOW;
   return r;
+}
+template <typename I>
+__device__ __forceinline__ I wrap_mul(I a, I b) {
+  using U = typename std::conditional<sizeof(I) == 4, uint32_t, uint64_t>::type;
+  return (I)((U)a * (U)b);
 }
 
 // Int#** (checked) and Int#&** (wrapping): binary exponentiation.
@@ -239,14 +243,14 @@ __device__ __forceinline__ I int_pow(I base, int64_t e, bool wrapping, uint32_t&
   while (e > 0) {
     if (e & 1) {
       if (wrapping) result = wrap_mul<I>(result, k);
-      else if (sizeof(I) == 4) result = (I)chk_mul32((int32_t)result, (int32_t)k, st);
-      else result = (I)chk_mul64((int64_t)result, (int64_t)k, st);
+      else if constexpr (sizeof(I) == 4) result = chk_mul32(result, k, st);
+      else result = chk_mul64(result, k, st);
     }
     e >>= 1;
     if (e > 0) {
       if (wrapping) k = wrap_mul<I>(k, k);
-      else if (sizeof(I) == 4) k = (I)chk_mul32((int32_t)k, (int32_t)k, st);
-      else k = (I)chk_mul64((int64_t)k, (int64_t)k, st);
+      else if constexpr (sizeof(I) == 4) k = chk_mul32(k, k, st);
+      else k = chk_mul64(k, k, st);
     }
   }
   return result;
@@ -267,269 +271,339 @@ __device__ __forceinline__ F powi(F a, int32_t b) {
   return recip ? (F)1 / r : r;
 }
 
-// ------------------------------------------------ one binary operation
-// a OP b in compute type T; b already converted to T unless op is POW with
-// an integer exponent (bt = the exponent's type).
-__device__ __forceinline__ uint64_t bin_op(int op, int T, int bt, uint64_t a, uint64_t b, uint32_t& st) {
-  switch (T) {
-    case PHCU_F32: {
-      float x = sf32(a);
-      if (op == PHCU_OP_POW && is_int_t(bt)) {
-        int32_t e = (bt == PHCU_I32) ? si32(b) : (int32_t)si64(b);
-        return pf32(powi<float>(x, e));
-      }
-      float y = sf32(b);
-      switch (op) {
-        case PHCU_OP_ADD: return pf32(x + y);
-        case PHCU_OP_SUB: return pf32(x - y);
-        case PHCU_OP_MUL: return pf32(x * y);
-        case PHCU_OP_DIV: return pf32(x / y);
-        case PHCU_OP_FLOORDIV: return pf32(floorf(x / y));
-        case PHCU_OP_MOD: {
-          if (y == 0.0f) { st |= PHCU_ST_DIVZERO; return pf32(0.0f); }
-          float q = floorf(x / y);
-          float mm = y * q;
-          return pf32(x - mm);
-        }
-        case PHCU_OP_POW: return pf32(powf(x, y));
-        case PHCU_OP_GT: return x > y;
-        case PHCU_OP_LT: return x < y;
-        case PHCU_OP_GE: return x >= y;
-        case PHCU_OP_LE: return x <= y;
-        case PHCU_OP_EQ: return x == y;
-        case PHCU_OP_CMP: return pi32((x > y) - (x < y));
-      }
-      return 0;
-    }
-    case PHCU_F64: {
-      double x = sf64(a);
-      if (op == PHCU_OP_POW && is_int_t(bt)) {
-        int32_t e = (bt == PHCU_I32) ? si32(b) : (int32_t)si64(b);
-        return pf64(powi<double>(x, e));
-      }
-      double y = sf64(b);
-      switch (op) {
-        case PHCU_OP_ADD: return pf64(x + y);
-        case PHCU_OP_SUB: return pf64(x - y);
-        case PHCU_OP_MUL: return pf64(x * y);
-        case PHCU_OP_DIV: return pf64(x / y);
-        case PHCU_OP_FLOORDIV: return pf64(floor(x / y));
-        case PHCU_OP_MOD: {
-          if (y == 0.0) { st |= PHCU_ST_DIVZERO; return pf64(0.0); }
-          double q = floor(x / y);
-          double mm = y * q;
-          return pf64(x - mm);
-        }
-        case PHCU_OP_POW: return pf64(pow(x, y));
-        case PHCU_OP_GT: return x > y;
-        case PHCU_OP_LT: return x < y;
-        case PHCU_OP_GE: return x >= y;
-        case PHCU_OP_LE: return x <= y;
-        case PHCU_OP_EQ: return x == y;
-        case PHCU_OP_CMP: return pi32((x > y) - (x < y));
-      }
-      return 0;
-    }
-    case PHCU_I32: {
-      int32_t x = si32(a), y = si32(b);
-      switch (op) {
-        case PHCU_OP_ADD: return pi32(chk_add32(x, y, st));
-        case PHCU_OP_SUB: return pi32(chk_sub32(x, y, st));
-        case PHCU_OP_MUL: return pi32(chk_mul32(x, y, st));
-        case PHCU_OP_DIV: return pf64((double)x / (double)y);
-        case PHCU_OP_FLOORDIV:
-          if (y == 0) { st |= PHCU_ST_DIVZERO; return 0; }
-          if (x == INT32_MIN && y == -1) { st |= PHCU_ST_OVERFLOW; return pi32(x); }
-          return pi32((int32_t)floordiv_i64(x, y));
-        case PHCU_OP_MOD:
-          if (y == 0) { st |= PHCU_ST_DIVZERO; return 0; }
-          if (y == -1) return 0;
-          return pi32((int32_t)floormod_i64(x, y));
-        case PHCU_OP_POW: return pi32(int_pow<int32_t>(x, y, false, st));
-        case PHCU_OP_WADD: return pi32((int32_t)((uint32_t)x + (uint32_t)y));
-        case PHCU_OP_WSUB: return pi32((int32_t)((uint32_t)x - (uint32_t)y));
-        case PHCU_OP_WMUL: return pi32(wrap_mul<int32_t>(x, y));
-        case PHCU_OP_WPOW: return pi32(int_pow<int32_t>(x, y, true, st));
-        case PHCU_OP_AND: return pi32(x & y);
-        case PHCU_OP_OR: return pi32(x | y);
-        case PHCU_OP_XOR: return pi32(x ^ y);
-        case PHCU_OP_GT: return x > y;
-        case PHCU_OP_LT: return x < y;
-        case PHCU_OP_GE: return x >= y;
-        case PHCU_OP_LE: return x <= y;
-        case PHCU_OP_EQ: return x == y;
-        case PHCU_OP_CMP: return pi32((x > y) - (x < y));
-      }
-      return 0;
-    }
-    case PHCU_I64: {
-      int64_t x = si64(a), y = si64(b);
-      switch (op) {
-        case PHCU_OP_ADD: return pi64(chk_add64(x, y, st));
-        case PHCU_OP_SUB: return pi64(chk_sub64(x, y, st));
-        case PHCU_OP_MUL: return pi64(chk_mul64(x, y, st));
-        case PHCU_OP_DIV: return pf64((double)x / (double)y);
-        case PHCU_OP_FLOORDIV:
-          if (y == 0) { st |= PHCU_ST_DIVZERO; return 0; }
-          if (x == INT64_MIN && y == -1) { st |= PHCU_ST_OVERFLOW; return pi64(x); }
-          return pi64(floordiv_i64(x, y));
-        case PHCU_OP_MOD:
-          if (y == 0) { st |= PHCU_ST_DIVZERO; return 0; }
-          if (y == -1) return 0;
-          return pi64(floormod_i64(x, y));
-        case PHCU_OP_POW: return pi64(int_pow<int64_t>(x, y, false, st));
-        case PHCU_OP_WADD: return pi64((int64_t)((uint64_t)x + (uint64_t)y));
-        case PHCU_OP_WSUB: return pi64((int64_t)((uint64_t)x - (uint64_t)y));
-        case PHCU_OP_WMUL: return pi64(wrap_mul<int64_t>(x, y));
-        case PHCU_OP_WPOW: return pi64(int_pow<int64_t>(x, y, true, st));
-        case PHCU_OP_AND: return pi64(x & y);
-        case PHCU_OP_OR: return pi64(x | y);
-        case PHCU_OP_XOR: return pi64(x ^ y);
-        case PHCU_OP_GT: return x > y;
-        case PHCU_OP_LT: return x < y;
-        case PHCU_OP_GE: return x >= y;
-        case PHCU_OP_LE: return x <= y;
-        case PHCU_OP_EQ: return x == y;
-        case PHCU_OP_CMP: return pi32((x > y) - (x < y));
-      }
-      return 0;
-    }
-    case PHCU_BOOL: {
-      uint64_t x = a & 1u, y = b & 1u;
-      switch (op) {
-        case PHCU_OP_AND: return x & y;
-        case PHCU_OP_OR: return x | y;
-        case PHCU_OP_XOR: return x ^ y;
-        case PHCU_OP_EQ: return x == y;
-      }
-      return 0;
-    }
+// ------------------------------------------------- vector op kernels
+// Each applies one binary operator to V element pairs (dispatch done once).
+#define PHCU_LOOP _Pragma("unroll") for (int v = 0; v < V; v++)
+
+template <typename S, int V>
+__device__ __forceinline__ void bin_f32(int op, int bt, S* a, const S* b, uint32_t& st) {
+  if (op == PHCU_OP_POW && is_int_t(bt)) {
+    PHCU_LOOP a[v] = pf32<S>(powi<float>(sf32(a[v]), bt == PHCU_I32 ? si32(b[v]) : (int32_t)(int64_t)b[v]));
+    return;
   }
-  return 0;
+  switch (op) {
+    case PHCU_OP_ADD: PHCU_LOOP a[v] = pf32<S>(sf32(a[v]) + sf32(b[v])); break;
+    case PHCU_OP_SUB: PHCU_LOOP a[v] = pf32<S>(sf32(a[v]) - sf32(b[v])); break;
+    case PHCU_OP_MUL: PHCU_LOOP a[v] = pf32<S>(sf32(a[v]) * sf32(b[v])); break;
+    case PHCU_OP_DIV: PHCU_LOOP a[v] = pf32<S>(sf32(a[v]) / sf32(b[v])); break;
+    case PHCU_OP_FLOORDIV: PHCU_LOOP a[v] = pf32<S>(floorf(sf32(a[v]) / sf32(b[v]))); break;
+    case PHCU_OP_MOD:
+      PHCU_LOOP {
+        const float x = sf32(a[v]), y = sf32(b[v]);
+        if (y == 0.0f) {
+          st |= PHCU_ST_DIVZERO;
+          a[v] = pf32<S>(0.0f);
+        } else {
+          const float q = floorf(x / y);
+          const float m = y * q;
+          a[v] = pf32<S>(x - m);
+        }
+      }
+      break;
+    case PHCU_OP_POW: PHCU_LOOP a[v] = pf32<S>(powf(sf32(a[v]), sf32(b[v]))); break;
+    case PHCU_OP_GT: PHCU_LOOP a[v] = sf32(a[v]) > sf32(b[v]); break;
+    case PHCU_OP_LT: PHCU_LOOP a[v] = sf32(a[v]) < sf32(b[v]); break;
+    case PHCU_OP_GE: PHCU_LOOP a[v] = sf32(a[v]) >= sf32(b[v]); break;
+    case PHCU_OP_LE: PHCU_LOOP a[v] = sf32(a[v]) <= sf32(b[v]); break;
+    case PHCU_OP_EQ: PHCU_LOOP a[v] = sf32(a[v]) == sf32(b[v]); break;
+    case PHCU_OP_CMP:
+      PHCU_LOOP {
+        const float x = sf32(a[v]), y = sf32(b[v]);
+        a[v] = pi32<S>((x > y) - (x < y));
+      }
+      break;
+  }
 }
 
-__device__ __forceinline__ uint64_t un_op(int op, int T, uint64_t a, uint32_t& st) {
+template <typename S, int V>
+__device__ __forceinline__ void bin_i32(int op, S* a, const S* b, uint32_t& st) {
   switch (op) {
-    case PHCU_I_POS: return a;
-    case PHCU_I_NEG:
-      switch (T) {
-        case PHCU_F32: return pf32(-sf32(a));
-        case PHCU_F64: return pf64(-sf64(a));
-        case PHCU_I32: {
-          int32_t x = si32(a);
-          if (x == INT32_MIN) { st |= PHCU_ST_OVERFLOW; return a; }
-          return pi32(-x);
-        }
-        case PHCU_I64: {
-          int64_t x = si64(a);
-          if (x == INT64_MIN) { st |= PHCU_ST_OVERFLOW; return a; }
-          return pi64(-x);
+    case PHCU_OP_ADD: PHCU_LOOP a[v] = pi32<S>(chk_add32(si32(a[v]), si32(b[v]), st)); break;
+    case PHCU_OP_SUB: PHCU_LOOP a[v] = pi32<S>(chk_sub32(si32(a[v]), si32(b[v]), st)); break;
+    case PHCU_OP_MUL: PHCU_LOOP a[v] = pi32<S>(chk_mul32(si32(a[v]), si32(b[v]), st)); break;
+    case PHCU_OP_DIV:
+      if constexpr (sizeof(S) == 8) {
+        PHCU_LOOP a[v] = pf64((double)si32(a[v]) / (double)si32(b[v]));
+      }
+      break;
+    case PHCU_OP_FLOORDIV:
+      PHCU_LOOP {
+        const int32_t x = si32(a[v]), y = si32(b[v]);
+        if (y == 0) {
+          st |= PHCU_ST_DIVZERO;
+          a[v] = 0;
+        } else if (x == INT32_MIN && y == -1) {
+          st |= PHCU_ST_OVERFLOW;
+        } else {
+          a[v] = pi32<S>((int32_t)floordiv_i64(x, y));
         }
       }
-      return a;
-    case PHCU_I_NOT:
-      if (T == PHCU_I32) return pi32(~si32(a));
-      if (T == PHCU_I64) return pi64(~si64(a));
-      return a;
+      break;
+    case PHCU_OP_MOD:
+      PHCU_LOOP {
+        const int32_t x = si32(a[v]), y = si32(b[v]);
+        if (y == 0) {
+          st |= PHCU_ST_DIVZERO;
+          a[v] = 0;
+        } else if (y == -1) {
+          a[v] = 0;
+        } else {
+          a[v] = pi32<S>((int32_t)floormod_i64(x, y));
+        }
+      }
+      break;
+    case PHCU_OP_POW: PHCU_LOOP a[v] = pi32<S>(int_pow<int32_t>(si32(a[v]), si32(b[v]), false, st)); break;
+    case PHCU_OP_WADD: PHCU_LOOP a[v] = pi32<S>((int32_t)((uint32_t)a[v] + (uint32_t)b[v])); break;
+    case PHCU_OP_WSUB: PHCU_LOOP a[v] = pi32<S>((int32_t)((uint32_t)a[v] - (uint32_t)b[v])); break;
+    case PHCU_OP_WMUL: PHCU_LOOP a[v] = pi32<S>((int32_t)((uint32_t)a[v] * (uint32_t)b[v])); break;
+    case PHCU_OP_WPOW: PHCU_LOOP a[v] = pi32<S>(int_pow<int32_t>(si32(a[v]), si32(b[v]), true, st)); break;
+    case PHCU_OP_AND: PHCU_LOOP a[v] = pi32<S>(si32(a[v]) & si32(b[v])); break;
+    case PHCU_OP_OR: PHCU_LOOP a[v] = pi32<S>(si32(a[v]) | si32(b[v])); break;
+    case PHCU_OP_XOR: PHCU_LOOP a[v] = pi32<S>(si32(a[v]) ^ si32(b[v])); break;
+    case PHCU_OP_GT: PHCU_LOOP a[v] = si32(a[v]) > si32(b[v]); break;
+    case PHCU_OP_LT: PHCU_LOOP a[v] = si32(a[v]) < si32(b[v]); break;
+    case PHCU_OP_GE: PHCU_LOOP a[v] = si32(a[v]) >= si32(b[v]); break;
+    case PHCU_OP_LE: PHCU_LOOP a[v] = si32(a[v]) <= si32(b[v]); break;
+    case PHCU_OP_EQ: PHCU_LOOP a[v] = si32(a[v]) == si32(b[v]); break;
+    case PHCU_OP_CMP:
+      PHCU_LOOP {
+        const int32_t x = si32(a[v]), y = si32(b[v]);
+        a[v] = pi32<S>((x > y) - (x < y));
+      }
+      break;
   }
-  return a;
+}
+
+template <int V>
+__device__ __forceinline__ void bin_f64(int op, int bt, uint64_t* a, const uint64_t* b, uint32_t& st) {
+  if (op == PHCU_OP_POW && is_int_t(bt)) {
+    PHCU_LOOP a[v] = pf64(powi<double>(sf64(a[v]), bt == PHCU_I32 ? si32(b[v]) : (int32_t)(int64_t)b[v]));
+    return;
+  }
+  switch (op) {
+    case PHCU_OP_ADD: PHCU_LOOP a[v] = pf64(sf64(a[v]) + sf64(b[v])); break;
+    case PHCU_OP_SUB: PHCU_LOOP a[v] = pf64(sf64(a[v]) - sf64(b[v])); break;
+    case PHCU_OP_MUL: PHCU_LOOP a[v] = pf64(sf64(a[v]) * sf64(b[v])); break;
+    case PHCU_OP_DIV: PHCU_LOOP a[v] = pf64(sf64(a[v]) / sf64(b[v])); break;
+    case PHCU_OP_FLOORDIV: PHCU_LOOP a[v] = pf64(floor(sf64(a[v]) / sf64(b[v]))); break;
+    case PHCU_OP_MOD:
+      PHCU_LOOP {
+        const double x = sf64(a[v]), y = sf64(b[v]);
+        if (y == 0.0) {
+          st |= PHCU_ST_DIVZERO;
+          a[v] = pf64(0.0);
+        } else {
+          const double q = floor(x / y);
+          const double m = y * q;
+          a[v] = pf64(x - m);
+        }
+      }
+      break;
+    case PHCU_OP_POW: PHCU_LOOP a[v] = pf64(pow(sf64(a[v]), sf64(b[v]))); break;
+    case PHCU_OP_GT: PHCU_LOOP a[v] = sf64(a[v]) > sf64(b[v]); break;
+    case PHCU_OP_LT: PHCU_LOOP a[v] = sf64(a[v]) < sf64(b[v]); break;
+    case PHCU_OP_GE: PHCU_LOOP a[v] = sf64(a[v]) >= sf64(b[v]); break;
+    case PHCU_OP_LE: PHCU_LOOP a[v] = sf64(a[v]) <= sf64(b[v]); break;
+    case PHCU_OP_EQ: PHCU_LOOP a[v] = sf64(a[v]) == sf64(b[v]); break;
+    case PHCU_OP_CMP:
+      PHCU_LOOP {
+        const double x = sf64(a[v]), y = sf64(b[v]);
+        a[v] = (uint64_t)(uint32_t)((x > y) - (x < y));
+      }
+      break;
+  }
+}
+
+template <int V>
+__device__ __forceinline__ void bin_i64(int op, uint64_t* a, const uint64_t* b, uint32_t& st) {
+  switch (op) {
+    case PHCU_OP_ADD: PHCU_LOOP a[v] = (uint64_t)chk_add64((int64_t)a[v], (int64_t)b[v], st); break;
+    case PHCU_OP_SUB: PHCU_LOOP a[v] = (uint64_t)chk_sub64((int64_t)a[v], (int64_t)b[v], st); break;
+    case PHCU_OP_MUL: PHCU_LOOP a[v] = (uint64_t)chk_mul64((int64_t)a[v], (int64_t)b[v], st); break;
+    case PHCU_OP_DIV: PHCU_LOOP a[v] = pf64((double)(int64_t)a[v] / (double)(int64_t)b[v]); break;
+    case PHCU_OP_FLOORDIV:
+      PHCU_LOOP {
+        const int64_t x = (int64_t)a[v], y = (int64_t)b[v];
+        if (y == 0) {
+          st |= PHCU_ST_DIVZERO;
+          a[v] = 0;
+        } else if (x == INT64_MIN && y == -1) {
+          st |= PHCU_ST_OVERFLOW;
+        } else {
+          a[v] = (uint64_t)floordiv_i64(x, y);
+        }
+      }
+      break;
+    case PHCU_OP_MOD:
+      PHCU_LOOP {
+        const int64_t x = (int64_t)a[v], y = (int64_t)b[v];
+        if (y == 0) {
+          st |= PHCU_ST_DIVZERO;
+          a[v] = 0;
+        } else if (y == -1) {
+          a[v] = 0;
+        } else {
+          a[v] = (uint64_t)floormod_i64(x, y);
+        }
+      }
+      break;
+    case PHCU_OP_POW: PHCU_LOOP a[v] = (uint64_t)int_pow<int64_t>((int64_t)a[v], (int64_t)b[v], false, st); break;
+    case PHCU_OP_WADD: PHCU_LOOP a[v] = a[v] + b[v]; break;
+    case PHCU_OP_WSUB: PHCU_LOOP a[v] = a[v] - b[v]; break;
+    case PHCU_OP_WMUL: PHCU_LOOP a[v] = a[v] * b[v]; break;
+    case PHCU_OP_WPOW: PHCU_LOOP a[v] = (uint64_t)int_pow<int64_t>((int64_t)a[v], (int64_t)b[v], true, st); break;
+    case PHCU_OP_AND: PHCU_LOOP a[v] = a[v] & b[v]; break;
+    case PHCU_OP_OR: PHCU_LOOP a[v] = a[v] | b[v]; break;
+    case PHCU_OP_XOR: PHCU_LOOP a[v] = a[v] ^ b[v]; break;
+    case PHCU_OP_GT: PHCU_LOOP a[v] = (int64_t)a[v] > (int64_t)b[v]; break;
+    case PHCU_OP_LT: PHCU_LOOP a[v] = (int64_t)a[v] < (int64_t)b[v]; break;
+    case PHCU_OP_GE: PHCU_LOOP a[v] = (int64_t)a[v] >= (int64_t)b[v]; break;
+    case PHCU_OP_LE: PHCU_LOOP a[v] = (int64_t)a[v] <= (int64_t)b[v]; break;
+    case PHCU_OP_EQ: PHCU_LOOP a[v] = a[v] == b[v]; break;
+    case PHCU_OP_CMP:
+      PHCU_LOOP {
+        const int64_t x = (int64_t)a[v], y = (int64_t)b[v];
+        a[v] = (uint64_t)(uint32_t)((x > y) - (x < y));
+      }
+      break;
+  }
+}
+
+template <typename S, int V>
+__device__ __forceinline__ void bin_bool(int op, S* a, const S* b) {
+  switch (op) {
+    case PHCU_OP_AND: PHCU_LOOP a[v] = (a[v] & b[v]) & 1u; break;
+    case PHCU_OP_OR: PHCU_LOOP a[v] = (a[v] | b[v]) & 1u; break;
+    case PHCU_OP_XOR: PHCU_LOOP a[v] = (a[v] ^ b[v]) & 1u; break;
+    case PHCU_OP_EQ: PHCU_LOOP a[v] = (a[v] & 1u) == (b[v] & 1u); break;
+  }
+}
+
+template <typename S, int V>
+__device__ __forceinline__ void un_vec(int op, int T, S* a, uint32_t& st) {
+  if (op == PHCU_I_POS) return;
+  if (op == PHCU_I_NEG) {
+    switch (T) {
+      case PHCU_F32: PHCU_LOOP a[v] = pf32<S>(-sf32(a[v])); break;
+      case PHCU_I32:
+        PHCU_LOOP {
+          const int32_t x = si32(a[v]);
+          if (x == INT32_MIN) st |= PHCU_ST_OVERFLOW;
+          else a[v] = pi32<S>(-x);
+        }
+        break;
+      case PHCU_F64:
+        if constexpr (sizeof(S) == 8) { PHCU_LOOP a[v] = pf64(-sf64(a[v])); }
+        break;
+      case PHCU_I64:
+        if constexpr (sizeof(S) == 8) {
+          PHCU_LOOP {
+            const int64_t x = (int64_t)a[v];
+            if (x == INT64_MIN) st |= PHCU_ST_OVERFLOW;
+            else a[v] = (uint64_t)(-x);
+          }
+        }
+        break;
+    }
+    return;
+  }
+  // NOT
+  if (T == PHCU_I32) {
+    PHCU_LOOP a[v] = pi32<S>(~si32(a[v]));
+  } else if (T == PHCU_I64) {
+    PHCU_LOOP a[v] = ~a[v];
+  }
+}
+
+template <typename S, int V>
+__device__ __forceinline__ void cvt_vec(S* a, int from, int to) {
+  if (from == to) return;
+  PHCU_LOOP a[v] = convert_slot<S>(a[v], from, to);
 }
 
 // ------------------------------------------------------ the interpreter
-template <int NIN, int VEC>
-__device__ __forceinline__ void run_program(const phcu_program_t& P, const uint64_t (&in)[NIN > 0 ? NIN : 1][VEC],
-                                            uint64_t (&acc)[VEC], uint32_t& st) {
-  uint64_t s0[VEC], s1[VEC];
-#pragma unroll
-  for (int v = 0; v < VEC; v++) { acc[v] = 0; s0[v] = 0; s1[v] = 0; }
+// Runs the program on V elements: in[k][v] are the loaded inputs, acc[v]
+// receives the result.  STASH=false instantiations require a program without
+// ST0/ST1 and without stash operands (the host checks).
+template <typename S, int NIN, int V, bool STASH>
+__device__ __forceinline__ void run_program(const phcu_program_t& P, const S (&in)[NIN > 0 ? NIN : 1][V], S (&acc)[V],
+                                            uint32_t& st) {
+  S s0[STASH ? V : 1], s1[STASH ? V : 1];
   const int ni = P.n_instr;
   for (int pc = 0; pc < ni; pc++) {
-    const phcu_instr_t& I = P.code[pc];
-    const int op = I.op;
-    if (op == PHCU_I_ST0) {
-#pragma unroll
-      for (int v = 0; v < VEC; v++) s0[v] = acc[v];
-      continue;
-    }
-    if (op == PHCU_I_ST1) {
-#pragma unroll
-      for (int v = 0; v < VEC; v++) s1[v] = acc[v];
-      continue;
+    const int op = P.code[pc].op;
+    const int T = P.code[pc].type;
+    if constexpr (STASH) {
+      if (op == PHCU_I_ST0) {
+        PHCU_LOOP s0[v] = acc[v];
+        continue;
+      }
+      if (op == PHCU_I_ST1) {
+        PHCU_LOOP s1[v] = acc[v];
+        continue;
+      }
     }
     if (op == PHCU_I_CVT) {
-      const int to = (int)I.imm.i;
-#pragma unroll
-      for (int v = 0; v < VEC; v++) acc[v] = convert_slot(acc[v], I.type, to);
+      cvt_vec<S, V>(acc, T, (int)P.code[pc].imm.i);
       continue;
     }
     if (op == PHCU_I_NEG || op == PHCU_I_NOT || op == PHCU_I_POS) {
-#pragma unroll
-      for (int v = 0; v < VEC; v++) acc[v] = un_op(op, I.type, acc[v], st);
+      un_vec<S, V>(op, T, acc, st);
       continue;
     }
     // operand B
-    uint64_t b[VEC];
-    switch (I.src) {
-      case PHCU_SRC_IMM: {
-        const uint64_t imm = (uint64_t)I.imm.i;
-#pragma unroll
-        for (int v = 0; v < VEC; v++) b[v] = imm;
-        break;
+    S b[V];
+    const int src = P.code[pc].src;
+    if (src == PHCU_SRC_IMM) {
+      const S imm = (S)(uint64_t)P.code[pc].imm.i;
+      PHCU_LOOP b[v] = imm;
+    } else if (STASH && src == PHCU_SRC_S0) {
+      PHCU_LOOP b[v] = s0[v];
+    } else if (STASH && src == PHCU_SRC_S1) {
+      PHCU_LOOP b[v] = s1[v];
+    } else {
+      PHCU_LOOP b[v] = in[0][v];
+      if constexpr (NIN > 1) {
+        if (src == 1) { PHCU_LOOP b[v] = in[1][v]; }
       }
-      case PHCU_SRC_S0:
-#pragma unroll
-        for (int v = 0; v < VEC; v++) b[v] = s0[v];
-        break;
-      case PHCU_SRC_S1:
-#pragma unroll
-        for (int v = 0; v < VEC; v++) b[v] = s1[v];
-        break;
-      default: {
-        const int k = I.src;
-#pragma unroll
-        for (int v = 0; v < VEC; v++) b[v] = in[0][v];
-        if constexpr (NIN > 1) {
-          if (k == 1) {
-#pragma unroll
-            for (int v = 0; v < VEC; v++) b[v] = in[1][v];
-          }
-        }
-        if constexpr (NIN > 2) {
-          if (k == 2) {
-#pragma unroll
-            for (int v = 0; v < VEC; v++) b[v] = in[2][v];
-          }
-        }
-        if constexpr (NIN > 3) {
-          if (k == 3) {
-#pragma unroll
-            for (int v = 0; v < VEC; v++) b[v] = in[3][v];
-          }
-        }
-        break;
+      if constexpr (NIN > 2) {
+        if (src == 2) { PHCU_LOOP b[v] = in[2][v]; }
+      }
+      if constexpr (NIN > 3) {
+        if (src == 3) { PHCU_LOOP b[v] = in[3][v]; }
       }
     }
-    if (op == PHCU_I_LD) {
-#pragma unroll
-      for (int v = 0; v < VEC; v++) acc[v] = convert_slot(b[v], I.btype, I.type);
-      continue;
-    }
-    const int T = I.type;
-    int bt = I.btype;
+    int bt = P.code[pc].btype;
     const bool int_exp = (op == PHCU_OP_POW) && is_float_t(T) && is_int_t(bt);
     if (!int_exp && bt != T) {
-#pragma unroll
-      for (int v = 0; v < VEC; v++) b[v] = convert_slot(b[v], bt, T);
+      cvt_vec<S, V>(b, bt, T);
       bt = T;
     }
-    if (I.flags & 1) {
-#pragma unroll
-      for (int v = 0; v < VEC; v++) acc[v] = bin_op(op, T, bt, b[v], acc[v], st);
-    } else {
-#pragma unroll
-      for (int v = 0; v < VEC; v++) acc[v] = bin_op(op, T, bt, acc[v], b[v], st);
+    if (op == PHCU_I_LD) {
+      PHCU_LOOP acc[v] = b[v];
+      continue;
+    }
+    if (P.code[pc].flags & 1) {  // ACC = B op ACC
+      PHCU_LOOP {
+        const S t = acc[v];
+        acc[v] = b[v];
+        b[v] = t;
+      }
+    }
+    switch (T) {
+      case PHCU_F32: bin_f32<S, V>(op, bt, acc, b, st); break;
+      case PHCU_I32: bin_i32<S, V>(op, acc, b, st); break;
+      case PHCU_BOOL: bin_bool<S, V>(op, acc, b); break;
+      case PHCU_F64:
+        if constexpr (sizeof(S) == 8) bin_f64<V>(op, bt, acc, b, st);
+        break;
+      case PHCU_I64:
+        if constexpr (sizeof(S) == 8) bin_i64<V>(op, acc, b, st);
+        break;
     }
   }
 }
+
+#undef PHCU_LOOP
 
 }  // namespace phcu

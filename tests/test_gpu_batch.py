@@ -1,0 +1,143 @@
+"""The persistent batched executor and the learned tuner on the GPU: every
+task of an uneven workload matches the oracle in all three execution modes;
+the MLP's hand-written gradients match the CPU oracle; the trained network
+picks configurations with less regret than the fixed default."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_task(ora, wl, i):
+    m = wl.meta[i]
+    v, w = wl.task_inputs(i)
+    v, w = np.ascontiguousarray(v), np.ascontiguousarray(w)
+    op = m["op"]
+    if op == "add":
+        return ora.map_binary(ora.OP_ADD, v, w)[0]
+    if op == "mul":
+        return ora.map_binary(ora.OP_MUL, v, w)[0]
+    if op == "chain":
+        t, _ = ora.map_binary_scalar(ora.OP_ADD, v, 4, ora.I32)
+        t, _ = ora.map_binary_scalar(ora.OP_POW, t, 2, ora.I32)
+        t, _ = ora.map_binary(ora.OP_MUL, t, w)
+        return ora.map_binary(ora.OP_SUB, t, v)[0]
+    if op == "sum":
+        if v.dtype == np.int32:
+            return ora.reduce(ora.RED_SUM, v, m["axis"])
+        return ora.reduce_f64(v, m["axis"])
+    return ora.reduce(ora.RED_ARGMAX, v, m["axis"], ora.I32)
+
+
+@pytest.fixture(scope="module")
+def small_workload(cu):
+    from phase_cu.batch import Workload
+
+    return Workload(n_tasks=400, seed=3, min_log2=4, max_log2=14, pool_log2=16)
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_batch_modes_match_oracle(cu, ora, small_workload, mode):
+    from phase_cu import _abi
+    from phase_cu.batch import Batch
+
+    wl = small_workload
+    _abi.call("phcu_memset", wl.out.ptr, 0, wl.out.nbytes)
+    b = Batch(wl.tasks(), wl.programs)
+    b.launch(mode)
+    if mode == 2:
+        b.launch(mode)  # replay of the captured graph
+    cu.check_errors()
+    host = wl.download_outputs()
+    for i, m in enumerate(wl.meta):
+        got = np.asarray(wl.task_output(host, i)).reshape(-1)
+        exp = np.asarray(_oracle_task(ora, wl, i)).reshape(-1)
+        if m["op"] == "sum" and m["dtype"] == cu.Float32:
+            # tolerance: 1e-6 of the sum of magnitudes vs the FP64 oracle
+            v, _ = wl.task_inputs(i)
+            mag = np.asarray(ora.reduce_f64(np.abs(np.ascontiguousarray(v)), m["axis"])).reshape(-1)
+            assert np.all(np.abs(got - exp) <= 1e-6 * mag + 1e-30), (i, m)
+        else:
+            assert np.array_equal(got, exp.astype(got.dtype)), (i, m["op"], m["dtype"])
+    b.close()
+
+
+def test_batch_configs_do_not_change_results(cu, small_workload):
+    from phase_cu import _abi
+    from phase_cu.batch import Batch
+
+    wl = small_workload
+    ref = None
+    rng = np.random.default_rng(0)
+    for trial in range(3):
+        chunks = rng.choice([2048, 8192, 32768, 131072], len(wl.meta))
+        layouts = rng.integers(0, 2, len(wl.meta))
+        _abi.call("phcu_memset", wl.out.ptr, 0, wl.out.nbytes)
+        b = Batch(wl.tasks(chunks, layouts), wl.programs)
+        b.launch(0)
+        out = wl.download_outputs()
+        b.close()
+        if ref is None:
+            ref = out
+        else:
+            # argmax / integer results bit-identical; float sums may differ in the last bits
+            for i, m in enumerate(wl.meta):
+                a = wl.task_output(out, i)
+                r = wl.task_output(ref, i)
+                if m["op"] == "sum" and m["dtype"] == cu.Float32:
+                    assert np.allclose(a, r, rtol=1e-6, atol=1e-6)
+                else:
+                    assert np.array_equal(a, r)
+
+
+def test_mlp_gradient_matches_oracle(cu, ora):
+    from phase_cu.tuner import MLP
+
+    rng = np.random.default_rng(0)
+    net = MLP(seed=7)
+    p = net.get_params()
+    x = rng.standard_normal((100, 24)).astype(np.float32)
+    y = rng.standard_normal(100).astype(np.float32)
+    loss, g = net.grad(x, y)
+    oloss, og = ora.mlp_forward_backward(p, x, y)
+    assert abs(loss - oloss) <= 1e-4 * abs(oloss)
+    # tolerance: FP32 accumulation with atomics vs FP64 oracle
+    scale = np.max(np.abs(og))
+    assert np.max(np.abs(g - og)) <= 1e-4 * scale
+    y_hat = net.forward(x, normalise=False)
+    assert np.allclose(np.mean((y_hat - y) ** 2), oloss, rtol=1e-4)
+
+
+def test_mlp_training_reduces_loss(cu):
+    from phase_cu.tuner import MLP
+
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((2048, 24)).astype(np.float32)
+    w = rng.standard_normal(24).astype(np.float32)
+    y = (np.tanh(x @ w / 4) * 3 + 0.1 * x[:, 0] ** 2).astype(np.float32)
+    net = MLP(seed=3)
+    before = float(np.mean((net.forward(x) - y) ** 2))
+    after = net.train(x, y, epochs=60, batch=128, lr=3e-3)
+    assert after < 0.2 * before
+
+
+def test_learned_tuner_beats_default_config(cu, small_workload):
+    """Exhaustive timings of each task under every configuration train the MLP
+    on one half of the tasks; on the other half its picks have lower regret
+    than the fixed default configuration."""
+    from phase_cu import tuner
+
+    wl = small_workload
+    tasks = wl.tasks()
+    idx = [i for i, m in enumerate(wl.meta)]
+    times = np.stack([tuner.measure(tasks[i], wl.programs, reps=3) for i in idx])
+    feats = tuner.feature_matrix([tasks[i] for i in idx])
+    half = len(idx) // 2
+    net = tuner.MLP(seed=1)
+    net.train(feats[:half].reshape(-1, 24), np.log2(times[:half].reshape(-1)), epochs=200, batch=256, lr=2e-3)
+    picks, _ = net.pick(feats[half:])
+    test_t = times[half:]
+    r_mlp = tuner.regret(test_t, picks)
+    r_def = tuner.regret(test_t, np.full(len(test_t), tuner.DEFAULT_CONFIG))
+    print("regret mlp %.4f default %.4f" % (r_mlp, r_def))
+    assert r_mlp < r_def
