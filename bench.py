@@ -122,9 +122,28 @@ def device_arm(args):
         arrays[dt] = (a, b)
 
     def build_jobs(dev):
-        """Descriptors of every operation of one step (outputs preallocated)."""
+        return make_jobs(cu, A, dev, n)
+
+    def run_job(j):
+        execute_job(lib, A, j)
+
+    dev = {}
+    for dt, (a, b) in arrays.items():
+        Ad = cu.CuNArray.from_numpy(a)
+        Bd = cu.CuNArray.from_numpy(b)
+        Cd = cu.CuNArray.empty([256, 512, 512], Ad.dtype)
+        dev[dt] = (Ad, Bd, Cd)
+    jobs = build_jobs(dev)
+    step_bytes = sum(j[3] for j in jobs)
+    return _device_timed(args, cu, A, lib, arrays, dev, jobs, run_job, step_bytes)
+
+
+def make_jobs(cu, A, dev, n):
+    """Descriptors of every operation of one step (outputs preallocated).
+    dev maps dtype tag -> (A, B, C) device arrays."""
+    if True:
         jobs = []
-        for dt in ("f32", "i32"):
+        for dt in dev:
             A_, B_, C_ = dev[dt]
             es = 4
             ap = A_.view().permute(2, 0, 1)
@@ -148,23 +167,48 @@ def device_arm(args):
             jobs.append(("scatter", "copy", (mv._cview(), ap._cview()), 2 * n * es, [C_]))
         return jobs
 
-    def run_job(j):
-        name, kind, a, nbytes, _ = j
-        if kind == "copy":
-            rc = lib.phcu_copy(ctypes.byref(a[0]), ctypes.byref(a[1]))
-        else:
-            rc = lib.phcu_binary(a[0], ctypes.byref(a[1]), ctypes.byref(a[2]), ctypes.byref(a[3]))
-        if rc:
-            A.check(rc, name)
 
-    dev = {}
-    for dt, (a, b) in arrays.items():
-        Ad = cu.CuNArray.from_numpy(a)
-        Bd = cu.CuNArray.from_numpy(b)
-        Cd = cu.CuNArray.empty([256, 512, 512], Ad.dtype)
-        dev[dt] = (Ad, Bd, Cd)
-    jobs = build_jobs(dev)
-    step_bytes = sum(j[3] for j in jobs)
+def execute_job(lib, A, j):
+    name, kind, a, nbytes, _ = j
+    if kind == "copy":
+        rc = lib.phcu_copy(ctypes.byref(a[0]), ctypes.byref(a[1]))
+    else:
+        rc = lib.phcu_binary(a[0], ctypes.byref(a[1]), ctypes.byref(a[2]), ctypes.byref(a[3]))
+    if rc:
+        A.check(rc, name)
+
+
+def profile_class(args):
+    """Runs only the launches of one operation class of the step (Float32 or
+    Int32), a few times: the command profiled by ncu."""
+    import phase_cu as cu
+    from phase_cu import _abi as A
+    from phase_cu import synth
+
+    cu.init(0)
+    lib = A.load()
+    n = int(np.prod(SHAPE))
+    dt = args.profile_dtype
+    if dt == "f32":
+        a, b = synth.uniform_f32(SHAPE, seed=0), synth.uniform_f32(SHAPE, seed=0, start=n)
+    else:
+        a = synth.uniform_i32(SHAPE, seed=0, lo=-2 ** 20, hi=2 ** 20)
+        b = synth.uniform_i32(SHAPE, seed=0, lo=-2 ** 20, hi=2 ** 20, start=n)
+    Ad, Bd = cu.CuNArray.from_numpy(a), cu.CuNArray.from_numpy(b)
+    dev = {dt: (Ad, Bd, cu.CuNArray.empty([256, 512, 512], Ad.dtype))}
+    jobs = [j for j in make_jobs(cu, A, dev, n) if j[0] == args.profile_class]
+    for _ in range(args.warmup):
+        for j in jobs:
+            execute_job(lib, A, j)
+    for _ in range(args.steps):
+        for j in jobs:
+            execute_job(lib, A, j)
+    A.call("phcu_sync")
+    print("profiled %d launches of %s (%s)" % (len(jobs) * (args.warmup + args.steps), args.profile_class, dt))
+
+
+def _device_timed(args, cu, A, lib, arrays, dev, jobs, run_job, step_bytes):
+    n = int(np.prod(SHAPE))
 
     def timer():
         t = ctypes.c_void_p()
@@ -299,6 +343,152 @@ def e2e_leg(A, lib, arrays, dev_arrays, jobs, args, timer, stop, step_bytes):
             "path": "phcu_upload/phcu_copy/phcu_binary/phcu_download on pinned host buffers"}
 
 
+# --------------------------------------------------------- other configs
+def _ms(A, lib, fn, reps, flush=False):
+    """Median device time of fn() over reps (CUDA events on the library stream)."""
+    out = []
+    for _ in range(reps):
+        if flush:
+            A.check(lib.phcu_l2_flush())
+        t = ctypes.c_void_p()
+        A.check(lib.phcu_timer_start(ctypes.byref(t)))
+        fn()
+        ms = ctypes.c_float()
+        A.check(lib.phcu_timer_stop(t, ctypes.byref(ms)))
+        out.append(ms.value)
+    return statistics.median(out)
+
+
+def extra_configs(reps=5):
+    """The remaining workloads, each measured on its own (GB/s = algorithmic
+    bytes / median device time)."""
+    import phase_cu as cu
+    from phase_cu import _abi as A
+    from phase_cu import synth
+
+    lib = A.load()
+    res = {}
+    gb = lambda nbytes, ms: round(nbytes / (ms * 1e-3) / 1e9, 1)
+
+    # C1: 1024x1024 a+b, a*b, a[.., 1..2..-1]; 12 MiB fits L2, so L2 is flushed before each rep
+    c1 = {}
+    n = 1024 * 1024
+    for dt in ("f32", "i32"):
+        a = synth.uniform_f32([1024, 1024], 0) if dt == "f32" else synth.uniform_i32([1024, 1024], 0)
+        b = (synth.uniform_f32([1024, 1024], 0, start=n) if dt == "f32"
+             else synth.uniform_i32([1024, 1024], 0, start=n))
+        X, Y = cu.CuNArray.from_numpy(a), cu.CuNArray.from_numpy(b)
+        O = cu.CuNArray.empty([1024, 1024], X.dtype)
+        G = cu.CuNArray.empty([1024, 512], X.dtype)
+        xv, yv, ov = X._view(), Y._view(), O._view()
+        sv = X.view(slice(None), cu.R(1, -1, 2))._cview()
+        gv = G._view()
+        for name, op in (("add", A.OP_ADD), ("mul", A.OP_MUL if dt == "f32" else A.OP_WMUL)):
+            ms = _ms(A, lib, lambda: A.check(lib.phcu_binary(op, ctypes.byref(xv), ctypes.byref(yv),
+                                                             ctypes.byref(ov))), reps, flush=True)
+            c1["%s_%s" % (name, dt)] = {"ms": round(ms, 4), "gbs": gb(3 * n * 4, ms)}
+        ms = _ms(A, lib, lambda: A.check(lib.phcu_copy(ctypes.byref(gv), ctypes.byref(sv))), reps, flush=True)
+        c1["view_step2_%s" % dt] = {"ms": round(ms, 4), "gbs": gb(2 * (n // 2) * 4, ms)}
+    res["c1_plain_1024sq"] = c1
+
+    # C3: fused ((x+4)**2)*y - z over 64x128x128x64 lognormal, then reductions per axis
+    shape = [64, 128, 128, 64]
+    n3 = int(np.prod(shape))
+    x = cu.CuNArray.from_numpy(synth.lognormal_f32(shape, 0))
+    y = cu.CuNArray.from_numpy(synth.lognormal_f32(shape, 1))
+    z = cu.CuNArray.from_numpy(synth.lognormal_f32(shape, 2))
+    pv = x.process(lambda e: (e + 4) ** 2) * y - z
+    prog, _ = cu.compile_program(pv._expr, cu.Float32)
+    ins = (A.View * 3)(*[l._cview() for l in pv._leaves])
+    r = cu.CuNArray.empty(shape, cu.Float32)
+    rv = r._view()
+    ms = _ms(A, lib, lambda: A.check(lib.phcu_eval(ctypes.byref(prog), ins, 3, ctypes.byref(rv))), reps)
+    c3 = {"fused_chain": {"ms": round(ms, 4), "gbs": gb(4 * n3 * 4, ms), "kernels": 1,
+                          "unfused_bytes": 10 * n3 * 4}}
+    for k in range(4):
+        oshape = shape[:k] + shape[k + 1:]
+        for name, op, odt in (("sum", A.RED_SUM, cu.Float32), ("max", A.RED_MAX, cu.Float32),
+                              ("argmax", A.RED_ARGMAX, cu.Int32)):
+            o = cu.CuNArray.empty(oshape, odt)
+            oview = o._view()
+            ms = _ms(A, lib, lambda: A.check(lib.phcu_reduce(op, ctypes.byref(rv), k, ctypes.byref(oview))), reps)
+            c3["%s_axis%d" % (name, k)] = {"ms": round(ms, 4), "gbs": gb(n3 * 4 + o.size * 4, ms)}
+    o1 = cu.CuNArray.empty([1], cu.Float32)
+    o1v = o1._view()
+    ms = _ms(A, lib, lambda: A.check(lib.phcu_reduce(A.RED_SUM, ctypes.byref(rv), -1, ctypes.byref(o1v))), reps)
+    c3["sum_all"] = {"ms": round(ms, 4), "gbs": gb(n3 * 4, ms)}
+    res["c3_fused_reduce"] = c3
+    del x, y, z, r
+
+    # C4: 4096x4096 heat, 1000 steps captured in one CUDA graph; FP32 error vs an FP64 run
+    from phase_cu import stencil
+
+    u0 = synth.gaussian_bumps_f32(4096, 4096, bumps=16, seed=0)
+    hs = stencil.Heat(u0)
+    ms = _ms(A, lib, lambda: hs.run(1000, use_graph=True), 3)
+    c4 = {"steps": 1000, "ms": round(ms, 3), "steps_per_s": round(1000 / (ms * 1e-3), 1),
+          "gbs_effective": gb(1000 * 2 * 4094 * 4094 * 4, ms),
+          "note": "two 64 MiB grids ping-pong; most of the working set stays in the 126 MB L2"}
+    c4["error_vs_fp64"] = stencil.error_vs_fp64(u0, (10, 100, 1000))
+    res["c4_heat_4096sq"] = c4
+
+    # C5: 10,000 uneven tasks, one persistent launch vs per-op launches (and a graph of them)
+    res["c5_batched"] = batched_leg(reps)
+    return res
+
+
+def batched_leg(reps=5, n_tasks=10000):
+    import phase_cu as cu
+    from phase_cu import _abi as A
+    from phase_cu import tuner
+    from phase_cu.batch import Batch, Workload
+
+    lib = A.load()
+    wl = Workload(n_tasks=n_tasks, seed=0)
+    tasks = wl.tasks()
+    b = Batch(tasks, wl.programs)
+    info = b.info()
+    out = {"tasks": n_tasks, "items": info["items"], "bytes": info["bytes"]}
+    c0 = ctypes.c_uint64()
+    for mode, name in ((0, "persistent"), (1, "per_op"), (2, "per_op_graph")):
+        b.launch(mode)  # warm-up (mode 2 captures its graph here)
+        lib.phcu_launch_count(ctypes.byref(c0))
+        before = c0.value
+        ms = _ms(A, lib, lambda: b.launch(mode), reps)
+        lib.phcu_launch_count(ctypes.byref(c0))
+        out[name] = {"ms": round(ms, 3), "ops_per_s": round(n_tasks / (ms * 1e-3), 1),
+                     "gbs": round(info["bytes"] / (ms * 1e-3) / 1e9, 1),
+                     "launches_per_run": (c0.value - before) // max(1, reps)}
+    b.close()
+    out["speedup_vs_per_op"] = round(out["per_op"]["ms"] / out["persistent"]["ms"], 2)
+    # learned tuner: exhaustive timings of a sample train the MLP; it then picks
+    # per-task work-item sizes for the whole batch
+    rng = np.random.default_rng(0)
+    sample = rng.choice(n_tasks, 480, replace=False)
+    times = np.stack([tuner.measure(tasks[i], wl.programs, reps=3) for i in sample])
+    feats = tuner.feature_matrix([tasks[i] for i in sample])
+    half = len(sample) * 3 // 4
+    net = tuner.MLP(seed=1)
+    net.train(feats[:half].reshape(-1, 24), np.log2(times[:half].reshape(-1)), epochs=200, batch=256, lr=2e-3)
+    picks, _ = net.pick(feats[half:])
+    out["tuner"] = {"train_tasks": int(half), "test_tasks": int(len(sample) - half),
+                    "regret_mlp": round(tuner.regret(times[half:], picks), 4),
+                    "regret_default": round(tuner.regret(times[half:], np.full(len(picks), tuner.DEFAULT_CONFIG)),
+                                            4)}
+    allf = tuner.feature_matrix(tasks)
+    allpick, _ = net.pick(allf)
+    chunks = [[2048, 8192, 32768, 131072][c % 4] for c in allpick]
+    layouts = [c // 4 for c in allpick]
+    bt = Batch(wl.tasks(chunks, layouts), wl.programs)
+    bt.launch(0)
+    ms = _ms(A, lib, lambda: bt.launch(0), reps)
+    bt.close()
+    out["persistent_mlp_tuned"] = {"ms": round(ms, 3), "ops_per_s": round(n_tasks / (ms * 1e-3), 1),
+                                   "gbs": round(info["bytes"] / (ms * 1e-3) / 1e9, 1)}
+    out["speedup_tuned_vs_per_op"] = round(out["per_op"]["ms"] / ms, 2)
+    return out
+
+
 # ------------------------------------------------------------ CPU baseline
 def cpu_workload(nthreads, shape=CPU_SAMPLE_SHAPE):
     """The same step on the oracle (the reference's loops restated in C): one
@@ -379,7 +569,15 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-extra", action="store_true")
+    p.add_argument("--profile-class", default=None,
+                   help="run only one operation class (gather_permute, gather_reverse, binary_permute, "
+                        "binary_reverse, scatter) for profiling")
+    p.add_argument("--profile-dtype", default="f32")
     args = p.parse_args()
+    if args.profile_class:
+        profile_class(args)
+        return
     if args.impl == "reference":
         res, rank = reference_arm(args)
         if rank == 0 and res:
@@ -387,6 +585,8 @@ def main():
         return
     res, rank = device_arm(args)
     if rank == 0:
+        if not args.no_extra:
+            res["extra"] = extra_configs()
         if not args.no_cpu:
             res["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
         print(json.dumps(res), flush=True)

@@ -246,6 +246,9 @@ PHCU_API int32_t phcu_heat_step(const float* u, float* out, int64_t n, int64_t m
  * use_graph != 0 captures the steps once into a CUDA graph and replays it. */
 PHCU_API int32_t phcu_heat_run(float* u, float* tmp, int64_t n, int64_t m, float coef, int32_t steps,
                       int32_t use_graph);
+/* The same run in Float64 (the reference run the Float32 error is measured against). */
+PHCU_API int32_t phcu_heat_run_f64(double* u, double* tmp, int64_t n, int64_t m, double coef, int32_t steps,
+                                   int32_t use_graph);
 
 /* ------------------------------------------------------------------ graphs
  * Stream capture of a sequence of calls (no reference counterpart: replaces

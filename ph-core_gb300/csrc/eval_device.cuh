@@ -103,31 +103,40 @@ __device__ __forceinline__ void row_group(const EvalPlan& p, const phcu_program_
 }
 
 // ----------------------------------------------------------------- TILE
+constexpr int TILE_PER_THREAD = TILE * TILE / TILE_THREADS;  // 16
+
 // Loads this thread's 16 elements of a TILE x TILE block of one staged input
-// (coalesced along R) and writes them to the shared tile.
+// (coalesced along R).  Coordinates past the edge of a partial tile repeat the
+// last valid element, so every value the program sees is a real element (no
+// spurious status bits).
 template <typename S, int ES>
-__device__ __forceinline__ void stage_tile(const char* base, int64_t sr, int64_t sw, int64_t nr, int64_t nw, S* tile) {
-  constexpr int LD = TILE + 1;
+__device__ __forceinline__ void stage_load(const char* base, int64_t sr, int64_t sw, int64_t nr, int64_t nw,
+                                           S* v) {
   constexpr int NWARP = TILE_THREADS / 32;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  // coordinates past the edge of a partial tile repeat the last valid element,
-  // so every value the program sees is a real element (no spurious status bits)
-  S v[TILE / NWARP][TILE / 32];
 #pragma unroll
   for (int i = 0; i < TILE / NWARP; i++) {
     const int64_t w = min((int64_t)(warp + i * NWARP), nw - 1);
 #pragma unroll
     for (int j = 0; j < TILE / 32; j++) {
       const int64_t r = min((int64_t)(lane + 32 * j), nr - 1);
-      v[i][j] = ld_elem<S, ES>(base + (r * sr + w * sw) * ES);
+      v[i * (TILE / 32) + j] = ld_elem<S, ES>(base + (r * sr + w * sw) * ES);
     }
   }
+}
+
+template <typename S>
+__device__ __forceinline__ void stage_store(const S* v, S* tile) {
+  constexpr int LD = TILE + 1;
+  constexpr int NWARP = TILE_THREADS / 32;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
 #pragma unroll
   for (int i = 0; i < TILE / NWARP; i++) {
     const int w = warp + i * NWARP;
 #pragma unroll
-    for (int j = 0; j < TILE / 32; j++) tile[w * LD + lane + 32 * j] = v[i][j];
+    for (int j = 0; j < TILE / 32; j++) tile[w * LD + lane + 32 * j] = v[i * (TILE / 32) + j];
   }
 }
 
@@ -201,21 +210,29 @@ __device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_
   const int64_t nr = min((int64_t)TILE, p.sp.shape[R] - r0);
   const int64_t nw = min((int64_t)TILE, p.sp.shape[W] - w0);
 
-  // phase 1: staged inputs, coalesced along R
-  int slot = 0;
+  // phase 1: staged inputs, coalesced along R.  All inputs' loads are issued
+  // before any shared-memory store so their latencies overlap.
+  {
+    S v[NIN > 0 ? NIN : 1][TILE_PER_THREAD];
 #pragma unroll
-  for (int k = 0; k < NIN; k++) {
-    if (k >= p.nin || !(p.staged & (1u << k))) continue;
-    S* tile = smem + (size_t)slot * TILE * LD;
-    slot++;
-    const int64_t sr = p.in[k].stride[R], sw = p.in[k].stride[W];
-    switch (dtype_size(p.in[k].dtype)) {
-      case 4: stage_tile<S, 4>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 4, sr, sw, nr, nw, tile); break;
-      case 8:
-        if constexpr (sizeof(S) == 8)
-          stage_tile<S, 8>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 8, sr, sw, nr, nw, tile);
-        break;
-      default: stage_tile<S, 1>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw), sr, sw, nr, nw, tile);
+    for (int k = 0; k < NIN; k++) {
+      if (k >= p.nin || !(p.staged & (1u << k))) continue;
+      const int64_t sr = p.in[k].stride[R], sw = p.in[k].stride[W];
+      switch (dtype_size(p.in[k].dtype)) {
+        case 4: stage_load<S, 4>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 4, sr, sw, nr, nw, v[k]); break;
+        case 8:
+          if constexpr (sizeof(S) == 8)
+            stage_load<S, 8>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 8, sr, sw, nr, nw, v[k]);
+          break;
+        default: stage_load<S, 1>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw), sr, sw, nr, nw, v[k]);
+      }
+    }
+    int slot = 0;
+#pragma unroll
+    for (int k = 0; k < NIN; k++) {
+      if (k >= p.nin || !(p.staged & (1u << k))) continue;
+      stage_store<S>(v[k], smem + (size_t)slot * TILE * LD);
+      slot++;
     }
   }
   __syncthreads();

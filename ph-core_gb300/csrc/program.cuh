@@ -271,6 +271,70 @@ __device__ __forceinline__ F powi(F a, int32_t b) {
   return recip ? (F)1 / r : r;
 }
 
+// Crystal `Int32 / Int32` is `x.to_f64 / y.to_f64`: the IEEE double quotient,
+// correctly rounded to nearest-even.  GB300's FP64 rate makes a double
+// division cost about as much as reading the operands many times over, so the
+// quotient is computed exactly with integer long division instead: normalise
+// |x| and |y| so their quotient m lies in [1, 2), take three 24-bit digits of
+// the fraction (each estimated with an FP32 reciprocal and corrected by the
+// exact integer remainder), round the 72-bit fraction to 52 bits with a sticky
+// bit from the remainder, and assemble the double's bits.  Every |quotient| of
+// two non-zero Int32 lies in [2^-31, 2^31], so the result is always normal.
+__device__ __forceinline__ uint64_t int32_div_f64_bits(int32_t x, int32_t y) {
+  const uint64_t sign = (uint64_t)(((uint32_t)x ^ (uint32_t)y) >> 31) << 63;
+  const uint32_t a = x < 0 ? 0u - (uint32_t)x : (uint32_t)x;
+  const uint32_t b = y < 0 ? 0u - (uint32_t)y : (uint32_t)y;
+  if (b == 0) {
+    if (a == 0) return 0x7ff8000000000000ull;                                  // 0 / 0 = NaN
+    return ((uint64_t)((uint32_t)x >> 31) << 63) | 0x7ff0000000000000ull;        // x / 0 = +-Inf (sign of x)
+  }
+  if (a == 0) return (uint64_t)((uint32_t)y >> 31) << 63;                        // +0.0 / y = +-0.0
+  const int la = 31 - __clz(a), lb = 31 - __clz(b);
+  // a' and b' with the leading one at bit 31 (as 64-bit values)
+  uint64_t an = (uint64_t)a << (31 - la);
+  const uint64_t bn = (uint64_t)b << (31 - lb);
+  int e = la - lb;
+  if (an < bn) {
+    an <<= 1;
+    e -= 1;
+  }
+  // m = an / bn in [1, 2): integer part 1, remainder r < bn
+  uint64_t r = an - bn;
+  const float rcp = __frcp_rn((float)bn);
+  uint64_t frac = 0;  // 72 fraction bits, built from 3 digits of 24
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const uint64_t num = r << 24;  // r < 2^32, so num < 2^56
+    int64_t q = (int64_t)((float)num * rcp);
+    int64_t rem = (int64_t)num - q * (int64_t)bn;
+    while (rem < 0) {
+      q -= 1;
+      rem += (int64_t)bn;
+    }
+    while (rem >= (int64_t)bn) {
+      q += 1;
+      rem -= (int64_t)bn;
+    }
+    // the 3 digits fill 72 bits: keep the top 64 in frac, the rest folds into the sticky bit
+    if (d < 2) frac = (frac << 24) | (uint64_t)q;                    // 48 bits after two digits
+    else frac = (frac << 16) | ((uint64_t)q >> 8);                   // 64 bits
+    if (d == 2) r = (uint64_t)rem | ((uint64_t)q & 0xffu);           // sticky source
+    else r = (uint64_t)rem;
+  }
+  // frac holds the first 64 fraction bits; bits below go into sticky
+  uint64_t mant = frac >> 12;                  // 52 bits
+  const uint64_t guard = (frac >> 11) & 1u;
+  const bool sticky = ((frac & 0x7ffull) != 0) || (r != 0);
+  if (guard && (sticky || (mant & 1u))) {
+    mant += 1;
+    if (mant >> 52) {  // rounded up to 2.0
+      mant = 0;
+      e += 1;
+    }
+  }
+  return sign | ((uint64_t)(e + 1023) << 52) | mant;
+}
+
 // ------------------------------------------------- vector op kernels
 // Each applies one binary operator to V element pairs (dispatch done once).
 #define PHCU_LOOP _Pragma("unroll") for (int v = 0; v < V; v++)
@@ -323,7 +387,7 @@ __device__ __forceinline__ void bin_i32(int op, S* a, const S* b, uint32_t& st) 
     case PHCU_OP_MUL: PHCU_LOOP a[v] = pi32<S>(chk_mul32(si32(a[v]), si32(b[v]), st)); break;
     case PHCU_OP_DIV:
       if constexpr (sizeof(S) == 8) {
-        PHCU_LOOP a[v] = pf64((double)si32(a[v]) / (double)si32(b[v]));
+        PHCU_LOOP a[v] = int32_div_f64_bits(si32(a[v]), si32(b[v]));
       }
       break;
     case PHCU_OP_FLOORDIV:

@@ -219,6 +219,57 @@ def test_fastdiv_formula():
             assert (t + n) >> l == n // d, (n, d)
 
 
+def _int32_div_f64_bits(x, y):
+    """Restatement of the device's exact Int32 / Int32 -> Float64 long division
+    (integer digits; the device estimates each digit with an FP32 reciprocal
+    and corrects it with the exact remainder, which yields the same digit)."""
+    sign = ((x < 0) ^ (y < 0)) << 63
+    a, b = abs(x), abs(y)
+    if b == 0:
+        return 0x7FF8000000000000 if a == 0 else ((x < 0) << 63) | 0x7FF0000000000000
+    if a == 0:
+        return (y < 0) << 63
+    la, lb = a.bit_length() - 1, b.bit_length() - 1
+    an, bn, e = a << (31 - la), b << (31 - lb), la - lb
+    if an < bn:
+        an, e = an << 1, e - 1
+    r = an - bn
+    frac = 0
+    for d in range(3):
+        num = r << 24
+        q, rem = divmod(num, bn)
+        if d < 2:
+            frac = (frac << 24) | q
+            r = rem
+        else:
+            frac = (frac << 16) | (q >> 8)
+            r = rem | (q & 0xFF)
+    mant = frac >> 12
+    guard = (frac >> 11) & 1
+    sticky = (frac & 0x7FF) != 0 or r != 0
+    if guard and (sticky or (mant & 1)):
+        mant += 1
+        if mant >> 52:
+            mant, e = 0, e + 1
+    return sign | ((e + 1023) << 52) | mant
+
+
+def test_int32_division_to_float64_is_correctly_rounded():
+    import struct
+
+    rng = np.random.default_rng(4)
+    cases = [(7, 2), (-7, 2), (1, 3), (2 ** 31 - 1, 1), (-2 ** 31, 1), (-2 ** 31, -1), (1, 2 ** 31 - 1),
+             (-2 ** 31, 2 ** 31 - 1), (0, -5), (0, 5), (5, 0), (-5, 0), (0, 0), (2 ** 31 - 1, -2 ** 31), (3, 3)]
+    cases += [(int(a), int(b)) for a, b in rng.integers(-2 ** 31, 2 ** 31, (20000, 2))]
+    cases += [(int(a), int(b)) for a, b in rng.integers(-1000, 1000, (5000, 2))]
+    for x, y in cases:
+        if y == 0:
+            exp = 0x7FF8000000000000 if x == 0 else (0x7FF0000000000000 | ((x < 0) << 63))
+        else:
+            exp = struct.unpack("<Q", struct.pack("<d", float(x) / float(y)))[0]
+        assert _int32_div_f64_bits(x, y) == exp, (x, y)
+
+
 def _header_functions():
     with open(os.path.join(ROOT, "include", "phcuda.h")) as f:
         text = f.read()
