@@ -237,6 +237,20 @@ PHCU_API int32_t phcu_result_dtype(int32_t op, int32_t ta, int32_t tb, int32_t* 
  * as I32 or I64. */
 PHCU_API int32_t phcu_reduce(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_view_t* out);
 
+/* phcu_reduce for callers that cannot allocate device memory: a host that has
+ * handed all device memory to its own pool, an embedded runtime, or code that
+ * runs inside a region where cudaMalloc would synchronise or fail.  It has no
+ * counterpart in the reference (which has no device code); results equal
+ * phcu_reduce's.  Split reductions keep their partials in a static device
+ * array of 2^18 partials (4 MiB) that every GPU loading the library holds
+ * until the process exits; a reduction that would need more partials is
+ * rejected with PHCU_ERR_UNSUPPORTED (phcu_reduce handles it).  The first call
+ * on a device looks the array up (cudaGetSymbolAddress), so make that first
+ * call before any stream capture.  Every call shares the array: calls that
+ * overlap on the GPU (different streams, no ordering) race.  No call allocates
+ * or frees memory. */
+PHCU_API int32_t phcu_reduce_noalloc(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_view_t* out);
+
 /* Explicit 2-D heat step on an n x m Float32 grid (examples/heat_equation.cr:38-51
  * generalised to 2-D shifted views): out interior = c + (up+down+left+right-c*4)*coef
  * evaluated left to right without FMA; boundary copied.  u and out are

@@ -258,7 +258,9 @@ int32_t reduce_impl(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_
     size_t need = (size_t)a.S * (size_t)a.O;
     if (partial_buf) {
       if (need > partial_cap)
-        return fail(PHCU_ERR_INVALID, "reduction needs %zu partials, scratch holds %zu", need, partial_cap);
+        return fail(PHCU_ERR_UNSUPPORTED,
+                    "reduction needs %zu partials but the allocation-free scratch holds %zu; use phcu_reduce", need,
+                    partial_cap);
       a.partial = (Partial*)partial_buf;
     } else {
       PHCU_TRY(scratch_alloc(need * sizeof(Partial), &scratch));
@@ -270,10 +272,44 @@ int32_t reduce_impl(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_
   return rc;
 }
 
+// ------------------------------------------------ allocation-free variant
+// Scratch for phcu_reduce_noalloc: the partial results of split reductions.
+// It lives in the library's device image, so every GPU that loads the library
+// holds these 4 MiB until the process exits, and no call ever allocates.
+constexpr size_t NOALLOC_PARTIALS = size_t(1) << 18;
+static __device__ __align__(256) Partial g_noalloc_partials[NOALLOC_PARTIALS];
+
+// Device address of g_noalloc_partials, looked up once per device (the host
+// symbol is only a stand-in: it must never be handed to a kernel).
+static void* g_noalloc_addr[64] = {nullptr};
+
+static int32_t noalloc_scratch(void** out) {
+  int dev = 0;
+  PHCU_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(PHCU_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(reduction scratch)");
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return PHCU_OK;
+}
+
 }  // namespace phcu
 
 using namespace phcu;
 
 extern "C" int32_t phcu_reduce(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_view_t* out) {
   return reduce_impl(op, in, axis, out, nullptr, 0);
+}
+
+extern "C" int32_t phcu_reduce_noalloc(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_view_t* out) {
+  PHCU_TRY(require_ctx());
+  void* scratch = nullptr;
+  PHCU_TRY(noalloc_scratch(&scratch));
+  // Every split writes its own partials before the combine reads them, so the
+  // scratch needs no clearing between calls.
+  return reduce_impl(op, in, axis, out, scratch, NOALLOC_PARTIALS);
 }

@@ -132,6 +132,7 @@ _SIGS = [
     ("phcu_unary", [ctypes.c_int32, _P(View), _P(View)]),
     ("phcu_result_dtype", [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, _P(ctypes.c_int32)]),
     ("phcu_reduce", [ctypes.c_int32, _P(View), ctypes.c_int32, _P(View)]),
+    ("phcu_reduce_noalloc", [ctypes.c_int32, _P(View), ctypes.c_int32, _P(View)]),
     ("phcu_heat_step", [_vp, _vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_float]),
     ("phcu_heat_run", [_vp, _vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_float, ctypes.c_int32, ctypes.c_int32]),
     ("phcu_heat_run_f64", [_vp, _vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_double, ctypes.c_int32,
