@@ -64,7 +64,11 @@ __device__ __forceinline__ void batch_reduce_units(const RedArgs& a, int rmode, 
 
 template <int KIND, typename T>
 __device__ __forceinline__ void batch_combine(const RedArgs& a, uint32_t& st) {
-  for (int64_t o = threadIdx.x; o < a.O; o += blockDim.x) combine_one<T, KIND>(a, o, st);
+  if (a.S >= 32) {
+    for (int64_t o = 0; o < a.O; o++) combine_block<T, KIND>(a, o, st);  // uniform loop: all threads
+  } else {
+    for (int64_t o = threadIdx.x; o < a.O; o += blockDim.x) combine_one<T, KIND>(a, o, st);
+  }
 }
 
 __device__ __forceinline__ void dispatch_reduce(const RedArgs& a, int rmode, int64_t u0, int64_t u1, uint32_t& st) {

@@ -126,6 +126,39 @@ __device__ __forceinline__ void stage_load(const char* base, int64_t sr, int64_t
   }
 }
 
+// Asynchronous global -> shared copies (cp.async, no registers involved): the
+// staged tile of an input with 4- or 8-byte elements is copied element by
+// element, all copies of all inputs in flight before one wait.
+template <int ES>
+__device__ __forceinline__ void cp_async_elem(void* smem_dst, const void* gmem_src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  if constexpr (ES == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem_src));
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem_src));
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+template <typename S, int ES>
+__device__ __forceinline__ void stage_async(const char* base, int64_t sr, int64_t sw, int64_t nr, int64_t nw, S* tile) {
+  constexpr int LD = TILE + 1;
+  constexpr int NWARP = TILE_THREADS / 32;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < TILE / NWARP; i++) {
+    const int wt = warp + i * NWARP;
+    const int64_t w = min((int64_t)wt, nw - 1);
+#pragma unroll
+    for (int j = 0; j < TILE / 32; j++) {
+      const int rt = lane + 32 * j;
+      const int64_t r = min((int64_t)rt, nr - 1);
+      cp_async_elem<ES>(&tile[wt * LD + rt], base + (r * sr + w * sw) * ES);
+    }
+  }
+}
+
 template <typename S>
 __device__ __forceinline__ void stage_store(const S* v, S* tile) {
   constexpr int LD = TILE + 1;
@@ -185,7 +218,7 @@ __device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_
   const int R = p.raxis;
   constexpr int LD = TILE + 1;
   constexpr int NWARP = TILE_THREADS / 32;
-  constexpr int NI = (sizeof(S) == 4) ? TILE / NWARP : TILE / NWARP / 2;  // rows per pass
+  constexpr int NI = (sizeof(S) == 4) ? 4 : 2;  // rows per pass (8 or 4 elements per thread)
   constexpr int V = NI * (TILE / 32);
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -210,30 +243,31 @@ __device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_
   const int64_t nr = min((int64_t)TILE, p.sp.shape[R] - r0);
   const int64_t nw = min((int64_t)TILE, p.sp.shape[W] - w0);
 
-  // phase 1: staged inputs, coalesced along R.  All inputs' loads are issued
-  // before any shared-memory store so their latencies overlap.
+  // phase 1: staged inputs, coalesced along R.  4- and 8-byte elements go
+  // straight to shared memory with cp.async (every input's copies in flight
+  // at once, no registers); Bool goes through registers.
   {
-    S v[NIN > 0 ? NIN : 1][TILE_PER_THREAD];
-#pragma unroll
-    for (int k = 0; k < NIN; k++) {
-      if (k >= p.nin || !(p.staged & (1u << k))) continue;
-      const int64_t sr = p.in[k].stride[R], sw = p.in[k].stride[W];
-      switch (dtype_size(p.in[k].dtype)) {
-        case 4: stage_load<S, 4>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 4, sr, sw, nr, nw, v[k]); break;
-        case 8:
-          if constexpr (sizeof(S) == 8)
-            stage_load<S, 8>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 8, sr, sw, nr, nw, v[k]);
-          break;
-        default: stage_load<S, 1>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw), sr, sw, nr, nw, v[k]);
-      }
-    }
     int slot = 0;
 #pragma unroll
     for (int k = 0; k < NIN; k++) {
       if (k >= p.nin || !(p.staged & (1u << k))) continue;
-      stage_store<S>(v[k], smem + (size_t)slot * TILE * LD);
+      S* tile = smem + (size_t)slot * TILE * LD;
       slot++;
+      const int64_t sr = p.in[k].stride[R], sw = p.in[k].stride[W];
+      switch (dtype_size(p.in[k].dtype)) {
+        case 4: stage_async<S, 4>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 4, sr, sw, nr, nw, tile); break;
+        case 8:
+          if constexpr (sizeof(S) == 8)
+            stage_async<S, 8>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 8, sr, sw, nr, nw, tile);
+          break;
+        default: {
+          S v[TILE_PER_THREAD];
+          stage_load<S, 1>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw), sr, sw, nr, nw, v);
+          stage_store<S>(v, tile);
+        }
+      }
     }
+    cp_async_wait_all();
   }
   __syncthreads();
 

@@ -16,9 +16,10 @@ struct EvalArgs {
 constexpr int ROW_THREADS = 256;
 
 // ROW: each thread handles U grid-strided chunks of VEC elements per iteration
-// (16 elements with 32-bit slots, 8 with 64-bit slots).
+// (elements_per_thread below).  At least three blocks per SM: the kernels are
+// latency-bound when registers limit residency.
 template <typename S, int NIN, int VEC, int U, bool STASH, bool COPY>
-__global__ void __launch_bounds__(ROW_THREADS) eval_row_kernel(const __grid_constant__ EvalArgs A) {
+__global__ void __launch_bounds__(ROW_THREADS, 3) eval_row_kernel(const __grid_constant__ EvalArgs A) {
   const uint32_t nchunks = (uint32_t)(A.plan.sp.n / VEC);
   const uint32_t nthreads = gridDim.x * blockDim.x;
   uint32_t st = 0;
@@ -28,7 +29,7 @@ __global__ void __launch_bounds__(ROW_THREADS) eval_row_kernel(const __grid_cons
 }
 
 template <typename S, int NIN, bool STASH, bool COPY>
-__global__ void __launch_bounds__(TILE_THREADS) eval_tile_kernel(const __grid_constant__ EvalArgs A) {
+__global__ void __launch_bounds__(TILE_THREADS, 3) eval_tile_kernel(const __grid_constant__ EvalArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S* smem = reinterpret_cast<S*>(smem_raw);
   uint32_t st = 0;
@@ -53,9 +54,17 @@ static int32_t launch_grid(K kernel, const EvalArgs& A, uint64_t work_blocks, in
   return check_launch(what);
 }
 
+// Elements per thread per iteration: enough independent loads in flight
+// without pushing the register count past three resident blocks per SM
+// (plain copies carry no interpreter state; stash registers cost the most).
+template <typename S, bool STASH, bool COPY>
+constexpr int elements_per_thread() {
+  return COPY ? (sizeof(S) == 4 ? 16 : 8) : STASH ? 4 : (sizeof(S) == 4 ? 8 : 4);
+}
+
 template <typename S, int NIN, bool STASH, bool COPY>
 static int32_t launch_row(const EvalArgs& A) {
-  constexpr int E = sizeof(S) == 4 ? 16 : 8;  // elements per thread per iteration
+  constexpr int E = elements_per_thread<S, STASH, COPY>();
   const uint64_t n = (uint64_t)A.plan.sp.n;
   switch (A.plan.vec) {
     case 4: {
@@ -66,9 +75,10 @@ static int32_t launch_row(const EvalArgs& A) {
       const uint64_t wb = (n / 2 + ROW_THREADS * (E / 2) - 1) / (ROW_THREADS * (E / 2));
       return launch_grid(eval_row_kernel<S, NIN, 2, E / 2, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
     }
-    default: {
-      const uint64_t wb = (n + ROW_THREADS * E - 1) / (ROW_THREADS * E);
-      return launch_grid(eval_row_kernel<S, NIN, 1, E, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
+    default: {  // scalar chunks: each carries its own offsets, so half as many
+      constexpr int U1 = E / 2;
+      const uint64_t wb = (n + ROW_THREADS * U1 - 1) / (ROW_THREADS * U1);
+      return launch_grid(eval_row_kernel<S, NIN, 1, U1, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
     }
   }
 }

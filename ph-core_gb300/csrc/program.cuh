@@ -585,6 +585,52 @@ __device__ __forceinline__ void cvt_vec(S* a, int from, int to) {
   PHCU_LOOP a[v] = convert_slot<S>(a[v], from, to);
 }
 
+// x ** e for an exponent shared by all V elements (an immediate): the same
+// multiply sequence as powi(), with the loop control uniform across the warp.
+template <typename S, int V>
+__device__ __forceinline__ void powi_uniform(S* a, int T, int32_t e) {
+  const bool recip = e < 0;
+  if (T == PHCU_F32) {
+    float x[V], r[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      x[v] = sf32(a[v]);
+      r[v] = 1.0f;
+    }
+    for (int32_t b = e;;) {
+      if (b & 1) {
+#pragma unroll
+        for (int v = 0; v < V; v++) r[v] = r[v] * x[v];
+      }
+      b /= 2;
+      if (b == 0) break;
+#pragma unroll
+      for (int v = 0; v < V; v++) x[v] = x[v] * x[v];
+    }
+#pragma unroll
+    for (int v = 0; v < V; v++) a[v] = pf32<S>(recip ? 1.0f / r[v] : r[v]);
+  } else if constexpr (sizeof(S) == 8) {
+    double x[V], r[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      x[v] = sf64(a[v]);
+      r[v] = 1.0;
+    }
+    for (int32_t b = e;;) {
+      if (b & 1) {
+#pragma unroll
+        for (int v = 0; v < V; v++) r[v] = r[v] * x[v];
+      }
+      b /= 2;
+      if (b == 0) break;
+#pragma unroll
+      for (int v = 0; v < V; v++) x[v] = x[v] * x[v];
+    }
+#pragma unroll
+    for (int v = 0; v < V; v++) a[v] = pf64(recip ? 1.0 / r[v] : r[v]);
+  }
+}
+
 // ------------------------------------------------------ the interpreter
 // Runs the program on V elements: in[k][v] are the loaded inputs, acc[v]
 // receives the result.  STASH=false instantiations require a program without
@@ -615,9 +661,15 @@ __device__ __forceinline__ void run_program(const phcu_program_t& P, const S (&i
       un_vec<S, V>(op, T, acc, st);
       continue;
     }
+    const int src = P.code[pc].src;
+    if (op == PHCU_OP_POW && src == PHCU_SRC_IMM && is_float_t(T) && is_int_t(P.code[pc].btype) &&
+        !(P.code[pc].flags & 1)) {
+      const int64_t e = P.code[pc].imm.i;
+      powi_uniform<S, V>(acc, T, P.code[pc].btype == PHCU_I32 ? (int32_t)(uint32_t)e : (int32_t)e);
+      continue;
+    }
     // operand B
     S b[V];
-    const int src = P.code[pc].src;
     if (src == PHCU_SRC_IMM) {
       const S imm = (S)(uint64_t)P.code[pc].imm.i;
       PHCU_LOOP b[v] = imm;

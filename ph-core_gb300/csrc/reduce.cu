@@ -51,6 +51,14 @@ __global__ void __launch_bounds__(256) reduce_combine_kernel(const __grid_consta
   if (st) atomicOr(a.status, st);
 }
 
+// One block per output: used when each output has many partials.
+template <typename T, int KIND>
+__global__ void __launch_bounds__(256) reduce_combine_block_kernel(const __grid_constant__ RedArgs a) {
+  uint32_t st = 0;
+  for (int64_t o = blockIdx.x; o < a.O; o += gridDim.x) combine_block<T, KIND>(a, o, st);
+  if (st) atomicOr(a.status, st);
+}
+
 template <typename T, int KIND>
 static int32_t launch_typed(const RedArgs& a, const RedShape& sh) {
   Context& c = ctx();
@@ -73,9 +81,14 @@ static int32_t launch_typed(const RedArgs& a, const RedShape& sh) {
   count_launch();
   PHCU_TRY(check_launch("reduce kernel"));
   if (a.S > 1) {
-    int64_t cb = (a.O + threads - 1) / threads;
-    if (cb > cap) cb = cap;
-    reduce_combine_kernel<T, KIND><<<(unsigned)cb, threads, 0, c.stream>>>(a);
+    if (a.S >= 32) {
+      int64_t cb = a.O < cap ? a.O : cap;
+      reduce_combine_block_kernel<T, KIND><<<(unsigned)cb, threads, 0, c.stream>>>(a);
+    } else {
+      int64_t cb = (a.O + threads - 1) / threads;
+      if (cb > cap) cb = cap;
+      reduce_combine_kernel<T, KIND><<<(unsigned)cb, threads, 0, c.stream>>>(a);
+    }
     count_launch();
     PHCU_TRY(check_launch("reduce combine kernel"));
   }

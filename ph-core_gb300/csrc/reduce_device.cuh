@@ -393,6 +393,105 @@ __device__ __forceinline__ void combine_one(const RedArgs& a, int64_t o, uint32_
   }
 }
 
+// All threads of the block fold the S partials of output o (power-of-two
+// blockDim <= 256; every thread must call it).  Thread t folds partials
+// t, t + blockDim, ... in order; the per-thread results are merged in a fixed
+// tree, so the result does not depend on timing.  Thread 0 stores.
+template <typename T, int KIND>
+__device__ __forceinline__ void combine_block(const RedArgs& a, int64_t o, uint32_t& st) {
+  __shared__ double sh_v[256];
+  __shared__ double sh_c[256];
+  __shared__ long long sh_i[256];
+  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
+  const int t = threadIdx.x, nt = blockDim.x;
+  constexpr bool INT = std::is_same<T, int32_t>::value || std::is_same<T, long long>::value;
+  if (KIND == RK_SUM && INT) {
+    long long s = 0;
+    for (int64_t j = t; j < a.S; j += nt) s = (long long)((unsigned long long)s + (unsigned long long)a.partial[j * a.O + o].i);
+    sh_i[t] = s;
+    __syncthreads();
+    for (int w = nt / 2; w >= 1; w >>= 1) {
+      if (t < w) sh_i[t] = (long long)((unsigned long long)sh_i[t] + (unsigned long long)sh_i[t + w]);
+      __syncthreads();
+    }
+    if (t == 0) store_final(a, o, 0, 0, true, sh_i[0], 0, st);
+  } else if (KIND == RK_SUM) {
+    double s = 0.0, c = 0.0;
+    for (int64_t j = t; j < a.S; j += nt) {
+      const double x = a.partial[j * a.O + o].v;
+      const double u = s + x;
+      if (fabs(s) >= fabs(x)) c += (s - u) + x;
+      else c += (x - u) + s;
+      s = u;
+    }
+    sh_v[t] = s;
+    sh_c[t] = c;
+    __syncthreads();
+    for (int w = nt / 2; w >= 1; w >>= 1) {
+      if (t < w) {
+        const double x = sh_v[t], y = sh_v[t + w];
+        const double u = x + y;
+        const double bp = u - x;
+        const double e = (x - (u - bp)) + (y - bp);
+        sh_v[t] = u;
+        sh_c[t] = (sh_c[t] + sh_c[t + w]) + e;
+      }
+      __syncthreads();
+    }
+    if (t == 0) store_final(a, o, sh_v[0] + sh_c[0], 0, false, 0, 0, st);
+  } else {
+    ExtAcc<T> e;
+    e.init();
+    for (int64_t j = t; j < a.S; j += nt) {
+      const Partial& P = a.partial[j * a.O + o];
+      ExtAcc<T> q;
+      if constexpr (std::is_same<T, long long>::value) q.v = __double_as_longlong(P.v);
+      else q.v = (T)P.v;
+      q.i = P.i;
+      e.merge(q, is_max);
+    }
+    if constexpr (std::is_same<T, long long>::value) sh_v[t] = __longlong_as_double(e.v);
+    else sh_v[t] = (double)e.v;
+    sh_i[t] = e.i;
+    __syncthreads();
+    for (int w = nt / 2; w >= 1; w >>= 1) {
+      if (t < w) {
+        ExtAcc<T> x, y;
+        if constexpr (std::is_same<T, long long>::value) {
+          x.v = __double_as_longlong(sh_v[t]);
+          y.v = __double_as_longlong(sh_v[t + w]);
+        } else {
+          x.v = (T)sh_v[t];
+          y.v = (T)sh_v[t + w];
+        }
+        x.i = sh_i[t];
+        y.i = sh_i[t + w];
+        x.merge(y, is_max);
+        if constexpr (std::is_same<T, long long>::value) sh_v[t] = __longlong_as_double(x.v);
+        else sh_v[t] = (double)x.v;
+        sh_i[t] = x.i;
+      }
+      __syncthreads();
+    }
+    if (t == 0) {
+      long long idx = sh_i[0];
+      T v;
+      if constexpr (std::is_same<T, long long>::value) v = __double_as_longlong(sh_v[0]);
+      else v = (T)sh_v[0];
+      const T first = ld<T>(a.in + out_offset(a, (uint32_t)o) * (int64_t)sizeof(T));
+      if (idx < 0 || Lim<T>::nan(first)) {
+        idx = 0;
+        v = first;
+      }
+      double d;
+      long long l;
+      ext_parts<T>(v, d, l);
+      store_final(a, o, d, l, false, 0, idx, st);
+    }
+  }
+  __syncthreads();
+}
+
 // Host planning of one reduction (shared with the batched executor): fills
 // `a` (without scratch) and picks the launch shape.  Returns PHCU_OK, or an
 // error; *trivial is set when nothing needs to run (no outputs) and *empty_sum

@@ -30,17 +30,33 @@ __global__ void __launch_bounds__(HEAT_COLS) heat_step_kernel(const T* __restric
   const int lane = threadIdx.x & 31;
   const bool jin = j < m;
   const int64_t jc = jin ? j : m - 1;  // lanes past the edge still take part in the shuffles
-  T up = (i0 > 0) ? __ldg(u + (i0 - 1) * m + jc) : (T)0;
-  T c = __ldg(u + i0 * m + jc);
-#pragma unroll 4
+  // the whole column strip (rows i0-1 .. i0+HEAT_ROWS) is loaded up front, all
+  // loads in flight at once; the warp's edge lanes also load their outer
+  // neighbour column
+  T col[HEAT_ROWS + 2];
+#pragma unroll
+  for (int r = 0; r < HEAT_ROWS + 2; r++) {
+    const int64_t i = i0 - 1 + r;
+    col[r] = (i >= 0 && i < n) ? __ldg(u + i * m + jc) : (T)0;
+  }
+  T side[HEAT_ROWS];
+  const bool edge = (lane == 0) || (lane == 31);
+  const int64_t js = (lane == 0) ? jc - 1 : jc + 1;
+  const bool side_ok = edge && js >= 0 && js < m;
+#pragma unroll
+  for (int r = 0; r < HEAT_ROWS; r++) {
+    const int64_t i = i0 + r;
+    side[r] = (side_ok && i < n) ? __ldg(u + i * m + js) : (T)0;
+  }
+#pragma unroll
   for (int r = 0; r < HEAT_ROWS; r++) {
     const int64_t i = i0 + r;
     if (i >= n) break;  // uniform across the block
-    const T down = (i + 1 < n) ? __ldg(u + (i + 1) * m + jc) : (T)0;
+    const T up = col[r], c = col[r + 1], down = col[r + 2];
     T left = __shfl_up_sync(0xffffffffu, c, 1);
     T right = __shfl_down_sync(0xffffffffu, c, 1);
-    if (lane == 0) left = (jc > 0) ? __ldg(u + i * m + jc - 1) : (T)0;
-    if (lane == 31) right = (jc + 1 < m) ? __ldg(u + i * m + jc + 1) : (T)0;
+    if (lane == 0) left = side[r];
+    if (lane == 31) right = side[r];
     if (jin) {
       T res;
       if (i == 0 || i == n - 1 || j == 0 || j == m - 1) {
@@ -56,8 +72,6 @@ __global__ void __launch_bounds__(HEAT_COLS) heat_step_kernel(const T* __restric
       }
       out[i * m + j] = res;
     }
-    up = c;
-    c = down;
   }
 }
 
