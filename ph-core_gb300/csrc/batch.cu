@@ -63,9 +63,9 @@ __device__ __forceinline__ void batch_reduce_units(const RedArgs& a, int rmode, 
 }
 
 template <int KIND, typename T>
-__device__ __forceinline__ void batch_combine(const RedArgs& a, uint32_t& st) {
+__device__ __forceinline__ void batch_combine(const RedArgs& a, CombineScratch& cs, uint32_t& st) {
   if (a.S >= 32) {
-    for (int64_t o = 0; o < a.O; o++) combine_block<T, KIND>(a, o, st);  // uniform loop: all threads
+    for (int64_t o = 0; o < a.O; o++) combine_block<T, KIND>(a, o, cs, st);  // uniform loop: all threads
   } else {
     for (int64_t o = threadIdx.x; o < a.O; o += blockDim.x) combine_one<T, KIND>(a, o, st);
   }
@@ -92,24 +92,24 @@ __device__ __forceinline__ void dispatch_reduce(const RedArgs& a, int rmode, int
   }
 }
 
-__device__ __forceinline__ void dispatch_combine(const RedArgs& a, uint32_t& st) {
+__device__ __forceinline__ void dispatch_combine(const RedArgs& a, CombineScratch& cs, uint32_t& st) {
   const bool sum = a.op == PHCU_RED_SUM;
   switch (a.dtype) {
     case PHCU_F32:
-      if (sum) batch_combine<RK_SUM, float>(a, st);
-      else batch_combine<RK_EXT, float>(a, st);
+      if (sum) batch_combine<RK_SUM, float>(a, cs, st);
+      else batch_combine<RK_EXT, float>(a, cs, st);
       break;
     case PHCU_I32:
-      if (sum) batch_combine<RK_SUM, int32_t>(a, st);
-      else batch_combine<RK_EXT, int32_t>(a, st);
+      if (sum) batch_combine<RK_SUM, int32_t>(a, cs, st);
+      else batch_combine<RK_EXT, int32_t>(a, cs, st);
       break;
     case PHCU_F64:
-      if (sum) batch_combine<RK_SUM, double>(a, st);
-      else batch_combine<RK_EXT, double>(a, st);
+      if (sum) batch_combine<RK_SUM, double>(a, cs, st);
+      else batch_combine<RK_EXT, double>(a, cs, st);
       break;
     default:
-      if (sum) batch_combine<RK_SUM, long long>(a, st);
-      else batch_combine<RK_EXT, long long>(a, st);
+      if (sum) batch_combine<RK_SUM, long long>(a, cs, st);
+      else batch_combine<RK_EXT, long long>(a, cs, st);
   }
 }
 
@@ -125,15 +125,16 @@ struct BatchArgs {
 };
 
 template <typename S>
-__global__ void __launch_bounds__(BATCH_THREADS) batch_kernel(const __grid_constant__ BatchArgs A) {
+__global__ void __launch_bounds__(BATCH_THREADS, 2) batch_kernel(const __grid_constant__ BatchArgs A) {
   extern __shared__ __align__(16) unsigned char tiles_raw[];
   S* tiles = reinterpret_cast<S*>(tiles_raw);
-  constexpr int E = sizeof(S) == 4 ? 8 : 4;  // elements per thread per row pass
+  constexpr int E = 4;  // elements per thread per row pass (the kernel carries every code path)
   __shared__ __align__(16) unsigned char s_plan[sizeof(EvalPlan) > sizeof(RedArgs) ? sizeof(EvalPlan)
                                                                                     : sizeof(RedArgs)];
   __shared__ __align__(16) unsigned char s_prog[sizeof(phcu_program_t)];
   __shared__ long long s_item;
   __shared__ int s_flag;
+  __shared__ CombineScratch s_combine;
   uint32_t st = 0;
   const uint64_t t_start = global_ns();
   for (;;) {
@@ -200,7 +201,7 @@ __global__ void __launch_bounds__(BATCH_THREADS) batch_kernel(const __grid_const
         __syncthreads();
         if (s_flag) {
           __threadfence();
-          dispatch_combine(a, st);
+          dispatch_combine(a, s_combine, st);
         }
       }
     }
@@ -411,14 +412,24 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
   }
   b->smem = (size_t)b->max_staged * TILE * (TILE + 1) * (b->narrow ? 4 : 8);
   int per_sm = 0;
-  if (b->narrow) {
-    if (b->smem > 48 * 1024)
-      cudaFuncSetAttribute(batch_kernel<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<uint32_t>, BATCH_THREADS, b->smem);
-  } else {
-    if (b->smem > 48 * 1024)
-      cudaFuncSetAttribute(batch_kernel<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<uint64_t>, BATCH_THREADS, b->smem);
+  // static + dynamic shared memory above the default 48 KiB needs an opt-in
+  auto prepare_kernel = [&](const void* fn) -> int32_t {
+    cudaFuncAttributes fa;
+    cudaError_t e2 = cudaFuncGetAttributes(&fa, fn);
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFuncGetAttributes(batch_kernel)");
+    if (fa.sharedSizeBytes + b->smem > 48 * 1024) {
+      e2 = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
+      if (e2 != cudaSuccess) return cuda_fail(e2, "cudaFuncSetAttribute(batch_kernel)");
+    }
+    e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, BATCH_THREADS, b->smem);
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaOccupancyMaxActiveBlocksPerMultiprocessor(batch_kernel)");
+    return PHCU_OK;
+  };
+  int32_t prc = b->narrow ? prepare_kernel((const void*)batch_kernel<uint32_t>)
+                          : prepare_kernel((const void*)batch_kernel<uint64_t>);
+  if (prc != PHCU_OK) {
+    free_batch(b);
+    return prc;
   }
   if (per_sm < 1) per_sm = 1;
   b->grid = ctx().sm_count * per_sm;

@@ -54,8 +54,9 @@ __global__ void __launch_bounds__(256) reduce_combine_kernel(const __grid_consta
 // One block per output: used when each output has many partials.
 template <typename T, int KIND>
 __global__ void __launch_bounds__(256) reduce_combine_block_kernel(const __grid_constant__ RedArgs a) {
+  __shared__ CombineScratch cs;
   uint32_t st = 0;
-  for (int64_t o = blockIdx.x; o < a.O; o += gridDim.x) combine_block<T, KIND>(a, o, st);
+  for (int64_t o = blockIdx.x; o < a.O; o += gridDim.x) combine_block<T, KIND>(a, o, cs, st);
   if (st) atomicOr(a.status, st);
 }
 

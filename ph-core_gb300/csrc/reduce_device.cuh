@@ -393,15 +393,22 @@ __device__ __forceinline__ void combine_one(const RedArgs& a, int64_t o, uint32_
   }
 }
 
+// Shared scratch of combine_block (one per block, provided by the kernel).
+struct CombineScratch {
+  double v[256];
+  double c[256];
+  long long i[256];
+};
+
 // All threads of the block fold the S partials of output o (power-of-two
 // blockDim <= 256; every thread must call it).  Thread t folds partials
 // t, t + blockDim, ... in order; the per-thread results are merged in a fixed
 // tree, so the result does not depend on timing.  Thread 0 stores.
 template <typename T, int KIND>
-__device__ __forceinline__ void combine_block(const RedArgs& a, int64_t o, uint32_t& st) {
-  __shared__ double sh_v[256];
-  __shared__ double sh_c[256];
-  __shared__ long long sh_i[256];
+__device__ __forceinline__ void combine_block(const RedArgs& a, int64_t o, CombineScratch& cs, uint32_t& st) {
+  double* sh_v = cs.v;
+  double* sh_c = cs.c;
+  long long* sh_i = cs.i;
   const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
   const int t = threadIdx.x, nt = blockDim.x;
   constexpr bool INT = std::is_same<T, int32_t>::value || std::is_same<T, long long>::value;
