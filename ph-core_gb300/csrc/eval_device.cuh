@@ -254,6 +254,13 @@ __device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_
       S* tile = smem + (size_t)slot * TILE * LD;
       slot++;
       const int64_t sr = p.in[k].stride[R], sw = p.in[k].stride[W];
+      if (NIN == 1 && dtype_size(p.in[k].dtype) == 4) {
+        // a single input: 16 register loads in flight per thread beat element-wise cp.async
+        S v[TILE_PER_THREAD];
+        stage_load<S, 4>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 4, sr, sw, nr, nw, v);
+        stage_store<S>(v, tile);
+        continue;
+      }
       switch (dtype_size(p.in[k].dtype)) {
         case 4: stage_async<S, 4>(p.in[k].base + (off_in[k] + r0 * sr + w0 * sw) * 4, sr, sw, nr, nw, tile); break;
         case 8:

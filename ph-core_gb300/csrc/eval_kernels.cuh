@@ -19,7 +19,7 @@ constexpr int ROW_THREADS = 256;
 // (elements_per_thread below).  At least three blocks per SM: the kernels are
 // latency-bound when registers limit residency.
 template <typename S, int NIN, int VEC, int U, bool STASH, bool COPY>
-__global__ void __launch_bounds__(ROW_THREADS, 3) eval_row_kernel(const __grid_constant__ EvalArgs A) {
+__global__ void __launch_bounds__(ROW_THREADS, COPY ? 4 : 3) eval_row_kernel(const __grid_constant__ EvalArgs A) {
   const uint32_t nchunks = (uint32_t)(A.plan.sp.n / VEC);
   const uint32_t nthreads = gridDim.x * blockDim.x;
   uint32_t st = 0;
@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(ROW_THREADS, 3) eval_row_kernel(const __grid_c
 }
 
 template <typename S, int NIN, bool STASH, bool COPY>
-__global__ void __launch_bounds__(TILE_THREADS, 3) eval_tile_kernel(const __grid_constant__ EvalArgs A) {
+__global__ void __launch_bounds__(TILE_THREADS, COPY ? 4 : 3) eval_tile_kernel(const __grid_constant__ EvalArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S* smem = reinterpret_cast<S*>(smem_raw);
   uint32_t st = 0;
@@ -67,6 +67,15 @@ static int32_t launch_row(const EvalArgs& A) {
   constexpr int E = elements_per_thread<S, STASH, COPY>();
   const uint64_t n = (uint64_t)A.plan.sp.n;
   switch (A.plan.vec) {
+    case 8: {  // an 8-aligned plan is also 4-aligned: fall back when E < 8
+      if constexpr (E >= 8) {
+        const uint64_t wb = (n / 8 + ROW_THREADS * (E / 8) - 1) / (ROW_THREADS * (E / 8));
+        return launch_grid(eval_row_kernel<S, NIN, 8, E / 8, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
+      } else {
+        const uint64_t wb = (n / 4 + ROW_THREADS * (E / 4) - 1) / (ROW_THREADS * (E / 4));
+        return launch_grid(eval_row_kernel<S, NIN, 4, E / 4, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
+      }
+    }
     case 4: {
       const uint64_t wb = (n / 4 + ROW_THREADS * (E / 4) - 1) / (ROW_THREADS * (E / 4));
       return launch_grid(eval_row_kernel<S, NIN, 4, E / 4, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");

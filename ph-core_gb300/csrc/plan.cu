@@ -230,22 +230,43 @@ int32_t make_plan(const phcu_view_t* out, const phcu_view_t* const* ins, int nin
 
   p->mode = MODE_ROW;
   const int64_t L = m[W].n;
-  // elements per thread-chunk: a chunk never crosses a row
-  int vec = (L % 4 == 0) ? 4 : (L % 2 == 0) ? 2 : 1;
+  // Elements per thread-chunk (a chunk never crosses a row): the widest of
+  // 8, 4, 2 that divides the row and that every unit-stride operand can use
+  // with aligned vector accesses; if none fits them all, the widest dividing
+  // the row, with the misaligned operands on scalar accesses.
+  auto vec_ok = [&](const Operand* o, int v) {
+    const int es = dtype_size(o->dtype);
+    const int64_t sw = o->stride[W];
+    for (int a = 0; a < W; a++)
+      if (o->stride[a] % v != 0) return false;
+    int64_t align = (int64_t)v * es;
+    if (align > 16) align = 16;
+    uintptr_t lo = (uintptr_t)o->base;
+    if (sw == -1) lo -= (uintptr_t)((v - 1) * es);
+    return (lo % align) == 0;
+  };
+  int vec = 1;
+  for (int v : {8, 4, 2}) {
+    if (L % v != 0) continue;
+    bool all = true;
+    for (int k = 0; k < nops; k++) {
+      const int64_t sw = dst[k]->stride[W];
+      if ((sw == 1 || sw == -1) && !vec_ok(dst[k], v)) all = false;
+    }
+    if (all) {
+      vec = v;
+      break;
+    }
+  }
+  if (vec == 1) vec = (L % 4 == 0) ? 4 : (L % 2 == 0) ? 2 : 1;
   p->vec = vec;
   for (int k = 0; k < nops; k++) {
     Operand* o = dst[k];
-    int es = dtype_size(o->dtype);
-    int64_t sw = o->stride[W];
+    const int64_t sw = o->stride[W];
     if (vec == 1 || (sw != 1 && sw != -1)) continue;
-    bool outer_ok = true;
-    for (int a = 0; a < W; a++)
-      if (o->stride[a] % vec != 0) outer_ok = false;
-    int64_t align = (int64_t)vec * es;
-    if (align > 16) align = 16;
-    uintptr_t lo = (uintptr_t)o->base;
-    if (sw == -1) lo -= (uintptr_t)((vec - 1) * es);
-    if (outer_ok && (lo % align) == 0) o->vmode = (sw == 1) ? VM_VEC : VM_VEC_REV;
+    // an operand aligned for `vec` is also aligned for the 4-element chunks a
+    // kernel may use instead of 8
+    if (vec_ok(o, vec)) o->vmode = (sw == 1) ? VM_VEC : VM_VEC_REV;
   }
   p->nrows = n / L;
   p->lendiv.init((uint32_t)L);

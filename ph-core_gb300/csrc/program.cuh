@@ -50,7 +50,10 @@ __device__ __forceinline__ void st_elem(char* p, S v) {
 // VEC consecutive elements starting at p (aligned to min(16, VEC*ES) bytes).
 template <typename S, int ES, int VEC>
 __device__ __forceinline__ void ld_vec(const char* p, S* v) {
-  if constexpr (ES == 4) {
+  if constexpr (VEC == 8 && ES != 1) {  // two (ES=4) or four (ES=8) 16-byte accesses
+    ld_vec<S, ES, 4>(p, v);
+    ld_vec<S, ES, 4>(p + 4 * ES, v + 4);
+  } else if constexpr (ES == 4) {
     if constexpr (VEC == 4) {
       uint4 x = __ldg((const uint4*)p);
       v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
@@ -79,7 +82,10 @@ __device__ __forceinline__ void ld_vec(const char* p, S* v) {
 
 template <typename S, int ES, int VEC>
 __device__ __forceinline__ void st_vec(char* p, const S* v) {
-  if constexpr (ES == 4) {
+  if constexpr (VEC == 8 && ES != 1) {
+    st_vec<S, ES, 4>(p, v);
+    st_vec<S, ES, 4>(p + 4 * ES, v + 4);
+  } else if constexpr (ES == 4) {
     if constexpr (VEC == 4) *(uint4*)p = make_uint4((uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], (uint32_t)v[3]);
     else if constexpr (VEC == 2) *(uint2*)p = make_uint2((uint32_t)v[0], (uint32_t)v[1]);
     else *(uint32_t*)p = (uint32_t)v[0];

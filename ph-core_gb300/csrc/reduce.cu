@@ -34,6 +34,23 @@ __global__ void __launch_bounds__(256) reduce_group_kernel(const __grid_constant
   if (st) atomicOr(a.status, st);
 }
 
+// GROUP over four outputs per group (short contiguous reduced axes).
+template <typename T, int KIND, int G>
+__global__ void __launch_bounds__(256) reduce_group4_kernel(const __grid_constant__ RedArgs a) {
+  constexpr int NO = 4;
+  const int lane = threadIdx.x & 31;
+  const int glane = lane & (G - 1);
+  const int groups_per_block = blockDim.x / G;
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+  uint32_t st = 0;
+  const int64_t og = (a.O + NO - 1) / NO;
+  const int64_t nwork = og * a.S;
+  for (int64_t w = (int64_t)blockIdx.x * groups_per_block + threadIdx.x / G; w < nwork;
+       w += (int64_t)gridDim.x * groups_per_block)
+    group_multi<T, KIND, G, NO>(a, (w % og) * NO, w / og, glane, gmask, st);
+  if (st) atomicOr(a.status, st);
+}
+
 template <typename T, int KIND>
 __global__ void __launch_bounds__(256) reduce_column_kernel(const __grid_constant__ RedArgs a) {
   uint32_t st = 0;
@@ -64,12 +81,21 @@ template <typename T, int KIND>
 static int32_t launch_typed(const RedArgs& a, const RedShape& sh) {
   Context& c = ctx();
   const int threads = 256;
-  int64_t work_threads = (sh.mode == 0) ? a.O * a.S * sh.G : a.O * a.S;
+  // four outputs per group when the reduced axis is short and outputs are many
+  const bool four = sh.mode == 0 && a.K <= 8 * sh.G && a.O >= 4096;
+  int64_t work_threads = (sh.mode == 0) ? (four ? (a.O + 3) / 4 : a.O) * a.S * sh.G : a.O * a.S;
   int64_t blocks = (work_threads + threads - 1) / threads;
   int64_t cap = (int64_t)c.sm_count * 8 * 4;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
-  if (sh.mode == 0) {
+  if (four) {
+    switch (sh.G) {
+      case 32: reduce_group4_kernel<T, KIND, 32><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      case 16: reduce_group4_kernel<T, KIND, 16><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      case 8: reduce_group4_kernel<T, KIND, 8><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      default: reduce_group4_kernel<T, KIND, 4><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+    }
+  } else if (sh.mode == 0) {
     switch (sh.G) {
       case 32: reduce_group_kernel<T, KIND, 32><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
       case 16: reduce_group_kernel<T, KIND, 16><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;

@@ -149,9 +149,14 @@ struct ExtAcc {  // (v, i); i < 0 = no candidate yet
     if (a == b && ia < ib) return true;
     return false;
   }
+  // Elements reach one accumulator in increasing k, so a later element only
+  // wins on a strict improvement (ties keep the earlier index).
   __device__ __forceinline__ void add(T x, long long k, bool is_max) {
-    if (Lim<T>::nan(x)) return;
-    if (better(x, k, v, i, is_max)) { v = x; i = k; }
+    const bool take = !Lim<T>::nan(x) && (i < 0 || (is_max ? (x > v) : (x < v)));
+    if (take) {
+      v = x;
+      i = k;
+    }
   }
   __device__ __forceinline__ void merge(const ExtAcc& o, bool is_max) {
     if (better(o.v, o.i, v, i, is_max)) { v = o.v; i = o.i; }
@@ -306,6 +311,65 @@ __device__ __forceinline__ void group_one(const RedArgs& a, int64_t o, int64_t s
     else eacc.shfl(d, gmask, G, is_max);
   }
   if (glane == 0) finish<T, KIND>(a, o, split, sacc, eacc, st);
+}
+
+// GROUP over NO outputs at once (short contiguous axes): each lane keeps NO
+// accumulators so NO x 2 loads are in flight per step.
+template <typename T, int KIND, int G, int NO>
+__device__ __forceinline__ void group_multi(const RedArgs& a, int64_t o0, int64_t split, int glane, unsigned gmask,
+                                            uint32_t& st) {
+  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
+  const int64_t k0 = split * a.chunk;
+  const int64_t k1 = min(a.K, k0 + a.chunk);
+  const char* base[NO];
+  SumAcc<T> sacc[NO];
+  ExtAcc<T> eacc[NO];
+#pragma unroll
+  for (int q = 0; q < NO; q++) {
+    const int64_t o = min(o0 + q, a.O - 1);  // past the end: repeat the last output (not stored)
+    base[q] = a.in + out_offset(a, (uint32_t)o) * (int64_t)sizeof(T);
+    sacc[q].init();
+    eacc[q].init();
+  }
+  int64_t k = k0 + glane;
+  for (; k + G < k1; k += 2 * G) {
+    const int64_t ka = k_offset(a, (uint32_t)k) * (int64_t)sizeof(T);
+    const int64_t kb = k_offset(a, (uint32_t)(k + G)) * (int64_t)sizeof(T);
+    T x[NO], y[NO];
+#pragma unroll
+    for (int q = 0; q < NO; q++) {
+      x[q] = ld<T>(base[q] + ka);
+      y[q] = ld<T>(base[q] + kb);
+    }
+#pragma unroll
+    for (int q = 0; q < NO; q++) {
+      if (KIND == RK_SUM) {
+        sacc[q].add(x[q]);
+        sacc[q].add(y[q]);
+      } else {
+        eacc[q].add(x[q], k, is_max);
+        eacc[q].add(y[q], k + G, is_max);
+      }
+    }
+  }
+  if (k < k1) {
+    const int64_t ka = k_offset(a, (uint32_t)k) * (int64_t)sizeof(T);
+#pragma unroll
+    for (int q = 0; q < NO; q++) {
+      const T x = ld<T>(base[q] + ka);
+      if (KIND == RK_SUM) sacc[q].add(x);
+      else eacc[q].add(x, k, is_max);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NO; q++) {
+#pragma unroll
+    for (int d = G / 2; d >= 1; d >>= 1) {
+      if (KIND == RK_SUM) sacc[q].shfl(d, gmask, G);
+      else eacc[q].shfl(d, gmask, G, is_max);
+    }
+    if (glane == 0 && o0 + q < a.O) finish<T, KIND>(a, o0 + q, split, sacc[q], eacc[q], st);
+  }
 }
 
 // COLUMN: one thread reduces elements [k0, k1) of output o.
