@@ -174,20 +174,20 @@ __global__ void __launch_bounds__(BATCH_THREADS, 2) batch_kernel(const __grid_co
       switch (T.vec) {
         case 4:
           for (int64_t c = u0 + threadIdx.x; c < u1; c += (int64_t)step * (E / 4))
-            row_group<S, MAXIN, 4, E / 4, true, false>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
+            row_group<S, MAXIN, 4, E / 4, true, FAST_NONE>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
           break;
         case 2:
           for (int64_t c = u0 + threadIdx.x; c < u1; c += (int64_t)step * (E / 2))
-            row_group<S, MAXIN, 2, E / 2, true, false>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
+            row_group<S, MAXIN, 2, E / 2, true, FAST_NONE>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
           break;
         default:
           for (int64_t c = u0 + threadIdx.x; c < u1; c += (int64_t)step * E)
-            row_group<S, MAXIN, 1, E, true, false>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
+            row_group<S, MAXIN, 1, E, true, FAST_NONE>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
       }
     } else if (kind == BK_TILE) {
       const EvalPlan& p = *reinterpret_cast<const EvalPlan*>(s_plan);
       const phcu_program_t& prog = *reinterpret_cast<const phcu_program_t*>(s_prog);
-      for (int64_t t = u0; t < u1; t++) tile_body<S, MAXIN, true, false>(p, prog, (uint64_t)t, tiles, st);
+      for (int64_t t = u0; t < u1; t++) tile_body<S, MAXIN, true, FAST_NONE>(p, prog, (uint64_t)t, tiles, st);
     } else {
       const RedArgs& a = *reinterpret_cast<const RedArgs*>(s_plan);
       dispatch_reduce(a, T.rmode, u0, u1, st);
@@ -311,9 +311,10 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
         b->max_staged = std::max(b->max_staged, __builtin_popcount(bt.ep.staged));
       } else {
         bt.kind = BK_ROW;
-        bt.vec = bt.ep.vec;
-        bt.nunits = bt.ep.sp.n / bt.ep.vec;
-        bt.per_item = std::max<int64_t>(1, chunk / bt.ep.vec);
+        // the batch kernel walks chunks of at most 4 (an 8-aligned plan is 4-aligned)
+        bt.vec = std::min(bt.ep.vec, 4);
+        bt.nunits = bt.ep.sp.n / bt.vec;
+        bt.per_item = std::max<int64_t>(1, chunk / bt.vec);
       }
     } else if (t.kind == PHCU_TASK_REDUCE) {
       RedShape sh;
@@ -332,10 +333,10 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
           return rc;
         }
         bt.kind = BK_ROW;
-        bt.vec = bt.ep.vec;
+        bt.vec = std::min(bt.ep.vec, 4);
         bt.prog = zero_prog(t.out.dtype);
-        bt.nunits = bt.ep.sp.n / bt.ep.vec;
-        bt.per_item = std::max<int64_t>(1, chunk / bt.ep.vec);
+        bt.nunits = bt.ep.sp.n / bt.vec;
+        bt.per_item = std::max<int64_t>(1, chunk / bt.vec);
         bt.bytes = bt.ep.sp.n * dtype_size(t.out.dtype);
         if (dtype_size(t.out.dtype) == 8) b->narrow = false;
       } else {

@@ -15,9 +15,13 @@ namespace phcu {
 
 constexpr int TILE_THREADS = 256;
 
+// FAST selects how the per-element work runs: the interpreter (FAST_NONE), a
+// plain move (FAST_COPY) or an in-place binary operator (FAST_BINOP).
+enum : int { FAST_NONE = 0, FAST_COPY = 1, FAST_BINOP = 2 };
+
 // ----------------------------------------------------------------- ROW
 // U chunks of VEC consecutive elements: chunk u is c0 + u * cstep.
-template <typename S, int NIN, int VEC, int U, bool STASH, bool COPY>
+template <typename S, int NIN, int VEC, int U, bool STASH, int FAST>
 __device__ __forceinline__ void row_group(const EvalPlan& p, const phcu_program_t& prog, uint32_t c0, uint32_t cstep,
                                           uint32_t nchunks, uint32_t& st) {
   constexpr int V = VEC * U;
@@ -73,7 +77,11 @@ __device__ __forceinline__ void row_group(const EvalPlan& p, const phcu_program_
     }
   }
   S acc[V];
-  if constexpr (COPY) {
+  if constexpr (FAST == FAST_COPY) {
+#pragma unroll
+    for (int v = 0; v < V; v++) acc[v] = in[0][v];
+  } else if constexpr (FAST == FAST_BINOP && NIN >= 2) {
+    run_binop<S, V>(prog, in[0], in[1], st);
 #pragma unroll
     for (int v = 0; v < V; v++) acc[v] = in[0][v];
   } else {
@@ -211,14 +219,16 @@ __device__ __forceinline__ void tile_store(char* obase, int64_t so_r, int r_firs
 
 // One TILE x TILE tile t (every thread of the block takes part; contains
 // __syncthreads).  smem holds one TILE x (TILE+1) array of S per staged input.
-template <typename S, int NIN, bool STASH, bool COPY>
+template <typename S, int NIN, bool STASH, int FAST>
 __device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_t& prog, uint64_t t, S* smem,
                                           uint32_t& st) {
   const int W = p.sp.rank - 1;
   const int R = p.raxis;
   constexpr int LD = TILE + 1;
   constexpr int NWARP = TILE_THREADS / 32;
-  constexpr int NI = (sizeof(S) == 4) ? 4 : 2;  // rows per pass (8 or 4 elements per thread)
+  // rows per pass: 8 (16 elements per thread) for copies and in-place binary
+  // operators, 4 (8 elements) for interpreted programs; half with 64-bit slots
+  constexpr int NI = (FAST != FAST_NONE ? 8 : 4) / (sizeof(S) == 4 ? 1 : 2);
   constexpr int V = NI * (TILE / 32);
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -319,7 +329,11 @@ __device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_
       }
     }
     S acc[V];
-    if constexpr (COPY) {
+    if constexpr (FAST == FAST_COPY) {
+#pragma unroll
+      for (int v = 0; v < V; v++) acc[v] = in[0][v];
+    } else if constexpr (FAST == FAST_BINOP && NIN >= 2) {
+      run_binop<S, V>(prog, in[0], in[1], st);
 #pragma unroll
       for (int v = 0; v < V; v++) acc[v] = in[0][v];
     } else {
@@ -366,6 +380,21 @@ inline bool program_uses_stash(const phcu_program_t& P) {
 }
 
 // A plain move: one input, one LD of its own type into an output of that type.
+// [ACC = IN0 (its own type); ACC = ACC op IN1 (IN1 already of the compute
+// type, or an integer exponent); optional CVT]: runs in place (run_binop).
+inline bool program_is_binop(const phcu_program_t& P, const EvalPlan& plan) {
+  if (plan.nin != 2 || P.n_instr < 2 || P.n_instr > 3) return false;
+  const phcu_instr_t& a = P.code[0];
+  const phcu_instr_t& b = P.code[1];
+  if (a.op != PHCU_I_LD || a.src != 0 || a.type != a.btype || a.type != plan.in[0].dtype) return false;
+  if (b.op >= PHCU_OP_NBINARY || b.src != 1 || (b.flags & 1) || b.type != a.type || b.btype != plan.in[1].dtype)
+    return false;
+  const bool int_exp = b.op == PHCU_OP_POW && is_float_t(b.type) && is_int_t(b.btype);
+  if (!int_exp && b.btype != b.type) return false;
+  if (P.n_instr == 3 && P.code[2].op != PHCU_I_CVT) return false;
+  return true;
+}
+
 inline bool program_is_copy(const phcu_program_t& P, const EvalPlan& plan) {
   return plan.nin == 1 && P.n_instr == 1 && P.code[0].op == PHCU_I_LD && P.code[0].src == 0 &&
          P.code[0].type == P.code[0].btype && P.code[0].type == plan.in[0].dtype && P.out_type == plan.out.dtype &&

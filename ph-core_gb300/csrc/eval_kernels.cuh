@@ -15,26 +15,31 @@ struct EvalArgs {
 
 constexpr int ROW_THREADS = 256;
 
-// ROW: each thread handles U grid-strided chunks of VEC elements per iteration
-// (elements_per_thread below).  At least three blocks per SM: the kernels are
-// latency-bound when registers limit residency.
-template <typename S, int NIN, int VEC, int U, bool STASH, bool COPY>
-__global__ void __launch_bounds__(ROW_THREADS, COPY ? 4 : 3) eval_row_kernel(const __grid_constant__ EvalArgs A) {
+// Copies get four resident blocks per SM, everything else three: the kernels
+// are latency-bound when registers limit residency.
+template <int FAST>
+constexpr int min_blocks() {
+  return FAST == FAST_COPY ? 4 : 3;
+}
+
+// ROW: each thread handles U grid-strided chunks of VEC elements per iteration.
+template <typename S, int NIN, int VEC, int U, bool STASH, int FAST>
+__global__ void __launch_bounds__(ROW_THREADS, min_blocks<FAST>()) eval_row_kernel(const __grid_constant__ EvalArgs A) {
   const uint32_t nchunks = (uint32_t)(A.plan.sp.n / VEC);
   const uint32_t nthreads = gridDim.x * blockDim.x;
   uint32_t st = 0;
   for (uint32_t c0 = blockIdx.x * blockDim.x + threadIdx.x; c0 < nchunks; c0 += nthreads * U)
-    row_group<S, NIN, VEC, U, STASH, COPY>(A.plan, A.prog, c0, nthreads, nchunks, st);
+    row_group<S, NIN, VEC, U, STASH, FAST>(A.plan, A.prog, c0, nthreads, nchunks, st);
   if (st) report_status(A.status, st);
 }
 
-template <typename S, int NIN, bool STASH, bool COPY>
-__global__ void __launch_bounds__(TILE_THREADS, COPY ? 4 : 3) eval_tile_kernel(const __grid_constant__ EvalArgs A) {
+template <typename S, int NIN, bool STASH, int FAST>
+__global__ void __launch_bounds__(TILE_THREADS, min_blocks<FAST>()) eval_tile_kernel(const __grid_constant__ EvalArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S* smem = reinterpret_cast<S*>(smem_raw);
   uint32_t st = 0;
   const uint64_t ntiles = (uint64_t)A.plan.tiles_w * A.plan.tiles_r * A.plan.nbatch;
-  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) tile_body<S, NIN, STASH, COPY>(A.plan, A.prog, t, smem, st);
+  for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) tile_body<S, NIN, STASH, FAST>(A.plan, A.prog, t, smem, st);
   if (st) report_status(A.status, st);
 }
 
@@ -55,67 +60,57 @@ static int32_t launch_grid(K kernel, const EvalArgs& A, uint64_t work_blocks, in
 }
 
 // Elements per thread per iteration: enough independent loads in flight
-// without pushing the register count past three resident blocks per SM
-// (plain copies carry no interpreter state; stash registers cost the most).
-template <typename S, bool STASH, bool COPY>
+// without pushing the register count past the residency target (copies and
+// in-place binary operators carry no interpreter state; stash registers cost
+// the most).
+template <typename S, bool STASH, int FAST>
 constexpr int elements_per_thread() {
-  return COPY ? (sizeof(S) == 4 ? 16 : 8) : STASH ? 4 : (sizeof(S) == 4 ? 8 : 4);
+  return FAST != FAST_NONE ? (sizeof(S) == 4 ? 16 : 8) : STASH ? 4 : (sizeof(S) == 4 ? 8 : 4);
 }
 
-template <typename S, int NIN, bool STASH, bool COPY>
-static int32_t launch_row(const EvalArgs& A) {
-  constexpr int E = elements_per_thread<S, STASH, COPY>();
+template <typename S, int NIN, int VEC, bool STASH, int FAST>
+static int32_t launch_row_vec(const EvalArgs& A) {
+  constexpr int E = elements_per_thread<S, STASH, FAST>();
+  constexpr int U = (VEC == 1) ? (E / 2 > 0 ? E / 2 : 1) : (E / VEC > 0 ? E / VEC : 1);
   const uint64_t n = (uint64_t)A.plan.sp.n;
+  const uint64_t wb = (n / VEC + ROW_THREADS * U - 1) / (ROW_THREADS * U);
+  return launch_grid(eval_row_kernel<S, NIN, VEC, U, STASH, FAST>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
+}
+
+template <typename S, int NIN, bool STASH, int FAST>
+static int32_t launch_row(const EvalArgs& A) {
+  constexpr int E = elements_per_thread<S, STASH, FAST>();
   switch (A.plan.vec) {
-    case 8: {  // an 8-aligned plan is also 4-aligned: fall back when E < 8
-      if constexpr (E >= 8) {
-        const uint64_t wb = (n / 8 + ROW_THREADS * (E / 8) - 1) / (ROW_THREADS * (E / 8));
-        return launch_grid(eval_row_kernel<S, NIN, 8, E / 8, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
-      } else {
-        const uint64_t wb = (n / 4 + ROW_THREADS * (E / 4) - 1) / (ROW_THREADS * (E / 4));
-        return launch_grid(eval_row_kernel<S, NIN, 4, E / 4, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
-      }
-    }
-    case 4: {
-      const uint64_t wb = (n / 4 + ROW_THREADS * (E / 4) - 1) / (ROW_THREADS * (E / 4));
-      return launch_grid(eval_row_kernel<S, NIN, 4, E / 4, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
-    }
-    case 2: {
-      const uint64_t wb = (n / 2 + ROW_THREADS * (E / 2) - 1) / (ROW_THREADS * (E / 2));
-      return launch_grid(eval_row_kernel<S, NIN, 2, E / 2, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
-    }
-    default: {  // scalar chunks: each carries its own offsets, so half as many
-      constexpr int U1 = E / 2;
-      const uint64_t wb = (n + ROW_THREADS * U1 - 1) / (ROW_THREADS * U1);
-      return launch_grid(eval_row_kernel<S, NIN, 1, U1, STASH, COPY>, A, wb, ROW_THREADS, 0, "eval_row_kernel");
-    }
+    case 8:  // an 8-aligned plan is also 4-aligned: 4-element chunks when E < 8
+      if constexpr (E >= 8) return launch_row_vec<S, NIN, 8, STASH, FAST>(A);
+      else return launch_row_vec<S, NIN, 4, STASH, FAST>(A);
+    case 4: return launch_row_vec<S, NIN, 4, STASH, FAST>(A);
+    case 2: return launch_row_vec<S, NIN, 2, STASH, FAST>(A);
+    default: return launch_row_vec<S, NIN, 1, STASH, FAST>(A);
   }
 }
 
-template <typename S, int NIN, bool STASH, bool COPY>
+template <typename S, int NIN, bool STASH, int FAST>
 static int32_t launch_tile(const EvalArgs& A) {
   const size_t smem = tile_smem_bytes<S>(A.plan.staged);
   const uint64_t ntiles = (uint64_t)A.plan.tiles_w * A.plan.tiles_r * A.plan.nbatch;
-  return launch_grid(eval_tile_kernel<S, NIN, STASH, COPY>, A, ntiles, TILE_THREADS, smem, "eval_tile_kernel");
+  return launch_grid(eval_tile_kernel<S, NIN, STASH, FAST>, A, ntiles, TILE_THREADS, smem, "eval_tile_kernel");
 }
 
 template <typename S, int NIN>
 int32_t launch_eval_sn(const EvalArgs& A) {
   const bool stash = program_uses_stash(A.prog);
-  if (A.plan.mode == MODE_TILE) {
-    if constexpr (NIN == 1) {
-      if (program_is_copy(A.prog, A.plan)) return launch_tile<S, NIN, false, true>(A);
-    }
-    return stash ? launch_tile<S, NIN, true, false>(A) : launch_tile<S, NIN, false, false>(A);
-  }
+  const bool tile = A.plan.mode == MODE_TILE;
   if constexpr (NIN == 1) {
-    if (program_is_copy(A.prog, A.plan)) return launch_row<S, NIN, false, true>(A);
+    if (program_is_copy(A.prog, A.plan))
+      return tile ? launch_tile<S, NIN, false, FAST_COPY>(A) : launch_row<S, NIN, false, FAST_COPY>(A);
   }
-  return stash ? launch_row<S, NIN, true, false>(A) : launch_row<S, NIN, false, false>(A);
+  if constexpr (NIN == 2) {
+    if (program_is_binop(A.prog, A.plan))
+      return tile ? launch_tile<S, NIN, false, FAST_BINOP>(A) : launch_row<S, NIN, false, FAST_BINOP>(A);
+  }
+  if (tile) return stash ? launch_tile<S, NIN, true, FAST_NONE>(A) : launch_tile<S, NIN, false, FAST_NONE>(A);
+  return stash ? launch_row<S, NIN, true, FAST_NONE>(A) : launch_row<S, NIN, false, FAST_NONE>(A);
 }
-
-// defined in eval_inst_*.cu
-int32_t launch_eval_u32(const EvalArgs& A);
-int32_t launch_eval_u64(const EvalArgs& A);
 
 }  // namespace phcu

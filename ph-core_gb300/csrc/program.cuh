@@ -637,6 +637,25 @@ __device__ __forceinline__ void powi_uniform(S* a, int T, int32_t e) {
   }
 }
 
+// A plain binary program, [ACC = IN0; ACC = ACC op IN1; optional CVT], run in
+// place on input 0's registers (no accumulator or operand copies).
+template <typename S, int V>
+__device__ __forceinline__ void run_binop(const phcu_program_t& P, S* a, const S* b, uint32_t& st) {
+  const int op = P.code[1].op, T = P.code[1].type, bt = P.code[1].btype;
+  switch (T) {
+    case PHCU_F32: bin_f32<S, V>(op, bt, a, b, st); break;
+    case PHCU_I32: bin_i32<S, V>(op, a, b, st); break;
+    case PHCU_BOOL: bin_bool<S, V>(op, a, b); break;
+    case PHCU_F64:
+      if constexpr (sizeof(S) == 8) bin_f64<V>(op, bt, a, b, st);
+      break;
+    case PHCU_I64:
+      if constexpr (sizeof(S) == 8) bin_i64<V>(op, a, b, st);
+      break;
+  }
+  if (P.n_instr == 3) cvt_vec<S, V>(a, P.code[2].type, (int)P.code[2].imm.i);
+}
+
 // ------------------------------------------------------ the interpreter
 // Runs the program on V elements: in[k][v] are the loaded inputs, acc[v]
 // receives the result.  STASH=false instantiations require a program without
