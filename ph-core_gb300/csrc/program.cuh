@@ -280,12 +280,18 @@ __device__ __forceinline__ F powi(F a, int32_t b) {
 // Crystal `Int32 / Int32` is `x.to_f64 / y.to_f64`: the IEEE double quotient,
 // correctly rounded to nearest-even.  GB300's FP64 rate makes a double
 // division cost about as much as reading the operands many times over, so the
-// quotient is computed exactly with integer long division instead: normalise
-// |x| and |y| so their quotient m lies in [1, 2), take three 24-bit digits of
-// the fraction (each estimated with an FP32 reciprocal and corrected by the
-// exact integer remainder), round the 72-bit fraction to 52 bits with a sticky
-// bit from the remainder, and assemble the double's bits.  Every |quotient| of
-// two non-zero Int32 lies in [2^-31, 2^31], so the result is always normal.
+// quotient is computed exactly with 32-bit integer long division instead
+// (schoolbook division with estimated digits, Knuth TAOCP vol. 2, 4.3.1):
+// normalise |x| and |y| so their quotient m lies in [1, 2) and the divisor b'
+// in [2^30, 2^31), then take three 18-bit digits of the fraction.  Each digit
+// is estimated as round(r * 2^18 / b') from the top 23 bits of the remainder
+// r and an FP32 reciprocal of b'; the estimate is within 0.15 of the exact
+// real quotient, so after rounding it is the true digit or one above it, and
+// a single check of the sign of the new remainder (which then fits an int32)
+// corrects it.  The 54 fraction bits and a sticky bit from the last remainder
+// are rounded to 52 bits and assembled into the double's bits.  Every
+// |quotient| of two non-zero Int32 lies in [2^-31, 2^31], so the result is
+// always normal.
 __device__ __forceinline__ uint64_t int32_div_f64_bits(int32_t x, int32_t y) {
   const uint64_t sign = (uint64_t)(((uint32_t)x ^ (uint32_t)y) >> 31) << 63;
   const uint32_t a = x < 0 ? 0u - (uint32_t)x : (uint32_t)x;
@@ -296,49 +302,42 @@ __device__ __forceinline__ uint64_t int32_div_f64_bits(int32_t x, int32_t y) {
   }
   if (a == 0) return (uint64_t)((uint32_t)y >> 31) << 63;                        // +0.0 / y = +-0.0
   const int la = 31 - __clz(a), lb = 31 - __clz(b);
-  // a' and b' with the leading one at bit 31 (as 64-bit values)
-  uint64_t an = (uint64_t)a << (31 - la);
-  const uint64_t bn = (uint64_t)b << (31 - lb);
+  // a' and b' with the leading one at bit 30 (|Int32| <= 2^31 leaves bit 0 of a << (31 - la) clear)
+  uint32_t an = (a << (31 - la)) >> 1;
+  const uint32_t bn = (b << (31 - lb)) >> 1;
   int e = la - lb;
   if (an < bn) {
     an <<= 1;
     e -= 1;
   }
-  // m = an / bn in [1, 2): integer part 1, remainder r < bn
-  uint64_t r = an - bn;
-  const float rcp = __frcp_rn((float)bn);
-  uint64_t frac = 0;  // 72 fraction bits, built from 3 digits of 24
+  // m = an / bn in [1, 2): integer part 1, remainder r < bn < 2^31
+  uint32_t r = an - bn;
+  float rc;  // 2^26 / bn within 1.5 ulp: bn rounds to FP32 (0.5 ulp), rcp.approx adds at most 1 ulp
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rc) : "f"(__uint2float_rn(bn)));
+  rc *= 67108864.0f;
+  uint32_t dg[3];
 #pragma unroll
-  for (int d = 0; d < 3; d++) {
-    const uint64_t num = r << 24;  // r < 2^32, so num < 2^56
-    int64_t q = (int64_t)((float)num * rcp);
-    int64_t rem = (int64_t)num - q * (int64_t)bn;
-    while (rem < 0) {
+  for (int k = 0; k < 3; k++) {
+    // r >> 8 < 2^23 converts exactly through the 2^23 exponent; the dropped bits
+    // move the estimate by under 2^8 * 2^18 / 2^30 = 1/16
+    const float rh = __uint_as_float(0x4b000000u | (r >> 8)) - 8388608.0f;
+    // rounded to an integer by the 1.5 * 2^23 offset, read from the mantissa field
+    uint32_t q = __float_as_uint(__fmaf_rn(rh, rc, 12582912.0f)) & 0x3fffffu;
+    int32_t rem = (int32_t)((r << 18) - q * bn);  // exact: the true value lies in [-bn, bn)
+    if (rem < 0) {
       q -= 1;
-      rem += (int64_t)bn;
+      rem += (int32_t)bn;
     }
-    while (rem >= (int64_t)bn) {
-      q += 1;
-      rem -= (int64_t)bn;
-    }
-    // the 3 digits fill 72 bits: keep the top 64 in frac, the rest folds into the sticky bit
-    if (d < 2) frac = (frac << 24) | (uint64_t)q;                    // 48 bits after two digits
-    else frac = (frac << 16) | ((uint64_t)q >> 8);                   // 64 bits
-    if (d == 2) r = (uint64_t)rem | ((uint64_t)q & 0xffu);           // sticky source
-    else r = (uint64_t)rem;
+    dg[k] = q;
+    r = (uint32_t)rem;
   }
-  // frac holds the first 64 fraction bits; bits below go into sticky
-  uint64_t mant = frac >> 12;                  // 52 bits
-  const uint64_t guard = (frac >> 11) & 1u;
-  const bool sticky = ((frac & 0x7ffull) != 0) || (r != 0);
-  if (guard && (sticky || (mant & 1u))) {
-    mant += 1;
-    if (mant >> 52) {  // rounded up to 2.0
-      mant = 0;
-      e += 1;
-    }
-  }
-  return sign | ((uint64_t)(e + 1023) << 52) | mant;
+  // fraction bits f1..f54 = dg[0] dg[1] dg[2]; f53 is the guard bit, f54 and the remainder are sticky
+  uint64_t mant = ((uint64_t)dg[0] << 34) | ((uint64_t)dg[1] << 16) | (dg[2] >> 2);
+  const bool guard = (dg[2] >> 1) & 1u;
+  const bool sticky = (dg[2] & 1u) || r != 0;
+  mant += (guard && (sticky || (mant & 1u))) ? 1u : 0u;
+  // a carry out of the 52 mantissa bits (m rounded up to 2.0) moves into the exponent
+  return sign | (((uint64_t)(e + 1023) << 52) + mant);
 }
 
 // ------------------------------------------------- vector op kernels

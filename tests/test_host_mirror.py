@@ -220,9 +220,15 @@ def test_fastdiv_formula():
 
 
 def _int32_div_f64_bits(x, y):
-    """Restatement of the device's exact Int32 / Int32 -> Float64 long division
-    (integer digits; the device estimates each digit with an FP32 reciprocal
-    and corrects it with the exact remainder, which yields the same digit)."""
+    """Restatement of the device's exact Int32 / Int32 -> Float64 long division:
+    three 18-bit digits, each estimated in FP32 and corrected once by the sign
+    of the remainder.  The device's reciprocal is rcp.approx (within 1 ulp of
+    the correctly rounded one used here), so the mirror also checks that the
+    estimate stays within 0.25 of the exact digit quotient: a 1-ulp change of
+    the reciprocal moves it by under 0.05, which keeps the rounded estimate the
+    true digit or one above it."""
+    from fractions import Fraction
+
     sign = ((x < 0) ^ (y < 0)) << 63
     a, b = abs(x), abs(y)
     if b == 0:
@@ -230,28 +236,28 @@ def _int32_div_f64_bits(x, y):
     if a == 0:
         return (y < 0) << 63
     la, lb = a.bit_length() - 1, b.bit_length() - 1
-    an, bn, e = a << (31 - la), b << (31 - lb), la - lb
+    an, bn, e = (a << (31 - la)) >> 1, (b << (31 - lb)) >> 1, la - lb
     if an < bn:
         an, e = an << 1, e - 1
     r = an - bn
-    frac = 0
-    for d in range(3):
-        num = r << 24
-        q, rem = divmod(num, bn)
-        if d < 2:
-            frac = (frac << 24) | q
-            r = rem
-        else:
-            frac = (frac << 16) | (q >> 8)
-            r = rem | (q & 0xFF)
-    mant = frac >> 12
-    guard = (frac >> 11) & 1
-    sticky = (frac & 0x7FF) != 0 or r != 0
+    rc = Fraction(float(np.float32(1.0) / np.float32(bn))) * 2 ** 26
+    dg = []
+    for _ in range(3):
+        t = Fraction(r >> 8) * rc  # the FMA's exact product
+        assert abs(t - Fraction(r << 18, bn)) < Fraction(1, 4)
+        q = round(t)  # round half to even, as the FP32 offset addition does
+        rem = (r << 18) - q * bn
+        assert -bn <= rem < bn
+        if rem < 0:
+            q, rem = q - 1, rem + bn
+        dg.append(q)
+        r = rem
+    mant = (dg[0] << 34) | (dg[1] << 16) | (dg[2] >> 2)
+    guard = (dg[2] >> 1) & 1
+    sticky = (dg[2] & 1) or r != 0
     if guard and (sticky or (mant & 1)):
         mant += 1
-        if mant >> 52:
-            mant, e = 0, e + 1
-    return sign | ((e + 1023) << 52) | mant
+    return sign | (((e + 1023) << 52) + mant)
 
 
 def test_int32_division_to_float64_is_correctly_rounded():
