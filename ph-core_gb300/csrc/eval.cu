@@ -14,6 +14,10 @@
 // Kernels are instantiated in eval_inst_*.cu; this file plans and dispatches.
 #include "eval_kernels.cuh"
 
+#include <cudaTypedefs.h>
+
+#include <cstdlib>
+
 namespace phcu {
 
 int32_t launch_eval_u32_lo(const EvalArgs& A);
@@ -21,8 +25,72 @@ int32_t launch_eval_u32_hi(const EvalArgs& A);
 int32_t launch_eval_u64_lo(const EvalArgs& A);
 int32_t launch_eval_u64_hi(const EvalArgs& A);
 
-int32_t launch_eval(const EvalArgs& A) {
-  if (A.plan.nin < 0 || A.plan.nin > MAXIN) return fail(PHCU_ERR_INVALID, "too many inputs (%d)", A.plan.nin);
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against libcuda); null when unavailable or when PHCU_TILE_TMA=0 selects the
+// register/cp.async staged tile path.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    const char* env = std::getenv("PHCU_TILE_TMA");
+    if (env && std::atoi(env) == 0) return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }
+    return (PFN_cuTensorMapEncodeTiled_v12000)f;
+  }();
+  return fn;
+}
+
+// Describes every staged input of a TILE plan as a tensor map over the plan's
+// axes [R, W, batch axes in order].  False (the staged tile path is used)
+// unless each staged input has 4-byte elements, unit stride along R, positive
+// strides that are multiples of 16 bytes elsewhere, a 16-byte aligned base,
+// and the plan has at most 5 axes.
+static bool encode_tile_maps(const EvalPlan& p, TmaMaps* m) {
+  if (p.mode != MODE_TILE || p.sp.rank < 2 || p.sp.rank > 5 || p.staged == 0) return false;
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return false;
+  const int W = p.sp.rank - 1, R = p.raxis;
+  int s = 0;
+  for (int k = 0; k < p.nin; k++) {
+    if (!(p.staged & (1u << k))) continue;
+    const Operand& o = p.in[k];
+    if (dtype_size(o.dtype) != 4 || o.stride[R] != 1 || ((uintptr_t)o.base & 15u) != 0) return false;
+    cuuint64_t dims[5], strides[4];
+    cuuint32_t box[5], estr[5] = {1, 1, 1, 1, 1};
+    dims[0] = (cuuint64_t)p.sp.shape[R];
+    box[0] = TMA_BOX_R;
+    int d = 1;
+    auto add_axis = [&](int a, cuuint32_t b) {
+      const int64_t sb = o.stride[a] * 4;
+      if (sb <= 0 || (sb & 15) != 0 || sb >= ((int64_t)1 << 40)) return false;
+      dims[d] = (cuuint64_t)p.sp.shape[a];
+      strides[d - 1] = (cuuint64_t)sb;
+      box[d] = b;
+      d++;
+      return true;
+    };
+    if (!add_axis(W, TILE)) return false;
+    for (int a = 0; a < W; a++)
+      if (a != R && !add_axis(a, 1)) return false;
+    const CUresult r = enc(&m->map[s], CU_TENSOR_MAP_DATA_TYPE_UINT32, (cuuint32_t)d, (void*)o.base, dims, strides,
+                           box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+    m->ndim = d;
+    s++;
+  }
+  return s > 0;
+}
+
+int32_t launch_eval(const EvalArgs& A0) {
+  if (A0.plan.nin < 0 || A0.plan.nin > MAXIN) return fail(PHCU_ERR_INVALID, "too many inputs (%d)", A0.plan.nin);
+  EvalArgs A = A0;
+  TmaMaps maps;
+  A.tma = encode_tile_maps(A.plan, &maps) ? &maps : nullptr;
   const bool narrow = program_is_32bit(A.prog, A.plan);
   if (narrow) return A.plan.nin <= 2 ? launch_eval_u32_lo(A) : launch_eval_u32_hi(A);
   return A.plan.nin <= 2 ? launch_eval_u64_lo(A) : launch_eval_u64_hi(A);

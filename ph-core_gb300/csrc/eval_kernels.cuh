@@ -7,10 +7,13 @@
 
 namespace phcu {
 
+struct TmaMaps;
+
 struct EvalArgs {
   EvalPlan plan;
   phcu_program_t prog;
   uint32_t* status;
+  const TmaMaps* tma = nullptr;  // host side: tensor maps of the staged inputs, when TMA can fetch them
 };
 
 constexpr int ROW_THREADS = 256;
@@ -97,19 +100,33 @@ static int32_t launch_tile(const EvalArgs& A) {
   return launch_grid(eval_tile_kernel<S, NIN, STASH, FAST>, A, ntiles, TILE_THREADS, smem, "eval_tile_kernel");
 }
 
+}  // namespace phcu
+
+#include "tile_tma.cuh"
+
+namespace phcu {
+
+template <typename S, int NIN, bool STASH, int FAST>
+static int32_t launch_tile_any(const EvalArgs& A) {
+  if constexpr (NIN > 0) {
+    if (A.tma) return launch_tma<S, NIN, STASH, FAST>(A);
+  }
+  return launch_tile<S, NIN, STASH, FAST>(A);
+}
+
 template <typename S, int NIN>
 int32_t launch_eval_sn(const EvalArgs& A) {
   const bool stash = program_uses_stash(A.prog);
   const bool tile = A.plan.mode == MODE_TILE;
   if constexpr (NIN == 1) {
     if (program_is_copy(A.prog, A.plan))
-      return tile ? launch_tile<S, NIN, false, FAST_COPY>(A) : launch_row<S, NIN, false, FAST_COPY>(A);
+      return tile ? launch_tile_any<S, NIN, false, FAST_COPY>(A) : launch_row<S, NIN, false, FAST_COPY>(A);
   }
   if constexpr (NIN == 2) {
     if (program_is_binop(A.prog, A.plan))
-      return tile ? launch_tile<S, NIN, false, FAST_BINOP>(A) : launch_row<S, NIN, false, FAST_BINOP>(A);
+      return tile ? launch_tile_any<S, NIN, false, FAST_BINOP>(A) : launch_row<S, NIN, false, FAST_BINOP>(A);
   }
-  if (tile) return stash ? launch_tile<S, NIN, true, FAST_NONE>(A) : launch_tile<S, NIN, false, FAST_NONE>(A);
+  if (tile) return stash ? launch_tile_any<S, NIN, true, FAST_NONE>(A) : launch_tile_any<S, NIN, false, FAST_NONE>(A);
   return stash ? launch_row<S, NIN, true, FAST_NONE>(A) : launch_row<S, NIN, false, FAST_NONE>(A);
 }
 
