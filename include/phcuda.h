@@ -123,7 +123,9 @@ enum {
   PHCU_I_CVT = 67,  /* ACC = (imm.i type) ACC, ACC of `type` */
   PHCU_I_NEG = 68,
   PHCU_I_NOT = 69,
-  PHCU_I_POS = 70
+  PHCU_I_POS = 70,
+  PHCU_I_SEL = 71   /* ACC = (S0 & 1) ? B : ACC  (S0 holds a Bool mask; masked writes,
+                       multi_writable.cr:127-172, n_array.cr:510-551) */
 };
 enum { PHCU_SRC_IMM = 8, PHCU_SRC_S0 = 9, PHCU_SRC_S1 = 10 };
 

@@ -410,6 +410,26 @@ def scatter_scalar(dst, value):
     return dst.arr
 
 
+def set_mask(arr, mask, value):
+    """NArray#[]=(mask, value) / MultiWritable#set_mask (n_array.cr:510-551,
+    multi_writable.cr:155-172): walks the coordinates in lexicographic order
+    and writes value (a scalar, or the element of a same-shaped source at the
+    coordinate) where the mask holds true.  arr is modified in place.  A
+    Python loop: for the small cases of the parity tests."""
+    mask = np.asarray(mask)
+    if tuple(mask.shape) != tuple(arr.shape):
+        raise OracleError(ERR_DIM, "set_mask")
+    src = None
+    if not np.isscalar(value) and not (isinstance(value, np.ndarray) and value.ndim == 0):
+        src = np.asarray(value)
+        if tuple(src.shape) != tuple(arr.shape):
+            raise OracleError(ERR_SHAPE, "set_mask")
+    for coord in np.ndindex(*arr.shape):
+        if mask[coord]:
+            arr[coord] = src[coord] if src is not None else value
+    return arr
+
+
 def result_dtype(op, ta, tb):
     t = ctypes.c_int32()
     _chk(lib().ora_result_dtype(op, ta, tb, ctypes.byref(t)), "result_dtype")

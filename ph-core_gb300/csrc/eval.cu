@@ -45,9 +45,11 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // Describes every staged input of a TILE plan as a tensor map over the plan's
-// axes [R, W, batch axes in order].  False (the staged tile path is used)
-// unless each staged input has 4-byte elements, unit stride along R, positive
-// strides that are multiples of 16 bytes elsewhere, a 16-byte aligned base,
+// axes [R, W, batch axes in order].  A batch axis the input walks backwards
+// is described forwards from its last element, with its coordinate mirrored
+// in the kernel.  False (the staged tile path is used) unless each staged
+// input has 4-byte elements, unit stride along R, a positive stride along W,
+// strides that are multiples of 16 bytes, a 16-byte aligned first address,
 // and the plan has at most 5 axes.
 static bool encode_tile_maps(const EvalPlan& p, TmaMaps* m) {
   if (p.mode != MODE_TILE || p.sp.rank < 2 || p.sp.rank > 5 || p.staged == 0) return false;
@@ -58,29 +60,40 @@ static bool encode_tile_maps(const EvalPlan& p, TmaMaps* m) {
   for (int k = 0; k < p.nin; k++) {
     if (!(p.staged & (1u << k))) continue;
     const Operand& o = p.in[k];
-    if (dtype_size(o.dtype) != 4 || o.stride[R] != 1 || ((uintptr_t)o.base & 15u) != 0) return false;
+    if (dtype_size(o.dtype) != 4 || o.stride[R] != 1 || o.stride[W] <= 0) return false;
+    const char* first = o.base;
+    uint32_t flip = 0;
     cuuint64_t dims[5], strides[4];
     cuuint32_t box[5], estr[5] = {1, 1, 1, 1, 1};
     dims[0] = (cuuint64_t)p.sp.shape[R];
     box[0] = TMA_BOX_R;
+    m->ext[0] = (int32_t)p.sp.shape[R];
     int d = 1;
     auto add_axis = [&](int a, cuuint32_t b) {
-      const int64_t sb = o.stride[a] * 4;
-      if (sb <= 0 || (sb & 15) != 0 || sb >= ((int64_t)1 << 40)) return false;
+      int64_t sb = o.stride[a] * 4;
+      if (sb < 0) {  // walk it forwards from its last element
+        first += (p.sp.shape[a] - 1) * sb;
+        sb = -sb;
+        flip |= 1u << d;
+      }
+      if (sb == 0 || (sb & 15) != 0 || sb >= ((int64_t)1 << 40)) return false;
       dims[d] = (cuuint64_t)p.sp.shape[a];
       strides[d - 1] = (cuuint64_t)sb;
       box[d] = b;
+      m->ext[d] = (int32_t)p.sp.shape[a];
       d++;
       return true;
     };
     if (!add_axis(W, TILE)) return false;
     for (int a = 0; a < W; a++)
       if (a != R && !add_axis(a, 1)) return false;
-    const CUresult r = enc(&m->map[s], CU_TENSOR_MAP_DATA_TYPE_UINT32, (cuuint32_t)d, (void*)o.base, dims, strides,
+    if (((uintptr_t)first & 15u) != 0) return false;
+    const CUresult r = enc(&m->map[s], CU_TENSOR_MAP_DATA_TYPE_UINT32, (cuuint32_t)d, (void*)first, dims, strides,
                            box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return false;
     m->ndim = d;
+    m->flip[s] = flip;
     s++;
   }
   return s > 0;
@@ -119,7 +132,7 @@ static int32_t check_program(const phcu_program_t* prog, int nin) {
         return fail(PHCU_ERR_INVALID, "instruction %d: operand source %d not available", i, I.src);
       if (!dtype_valid(I.btype)) return fail(PHCU_ERR_INVALID, "instruction %d: bad operand type", i);
     }
-    if (!(I.op < PHCU_OP_NBINARY || (I.op >= PHCU_I_LD && I.op <= PHCU_I_POS)))
+    if (!(I.op < PHCU_OP_NBINARY || (I.op >= PHCU_I_LD && I.op <= PHCU_I_SEL)))
       return fail(PHCU_ERR_INVALID, "instruction %d: unknown opcode %d", i, I.op);
     if (I.op == PHCU_I_CVT && !dtype_valid((int)I.imm.i))
       return fail(PHCU_ERR_INVALID, "instruction %d: bad conversion target", i);

@@ -374,7 +374,7 @@ inline bool program_is_32bit(const phcu_program_t& P, const EvalPlan& plan) {
 inline bool program_uses_stash(const phcu_program_t& P) {
   for (int i = 0; i < P.n_instr; i++) {
     const phcu_instr_t& I = P.code[i];
-    if (I.op == PHCU_I_ST0 || I.op == PHCU_I_ST1) return true;
+    if (I.op == PHCU_I_ST0 || I.op == PHCU_I_ST1 || I.op == PHCU_I_SEL) return true;
   }
   return false;
 }

@@ -723,6 +723,12 @@ __device__ __forceinline__ void run_program(const phcu_program_t& P, const S (&i
       PHCU_LOOP acc[v] = b[v];
       continue;
     }
+    if constexpr (STASH) {
+      if (op == PHCU_I_SEL) {
+        PHCU_LOOP acc[v] = (s0[v] & 1u) ? b[v] : acc[v];
+        continue;
+      }
+    }
     if (P.code[pc].flags & 1) {  // ACC = B op ACC
       PHCU_LOOP {
         const S t = acc[v];

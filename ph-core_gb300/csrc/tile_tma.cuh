@@ -26,8 +26,10 @@ constexpr uint64_t TMA_WAIT_NS = 1000000000ull;           // give up on a copy a
 // Tensor maps of the staged inputs, in staging order (bit order of plan.staged).
 struct TmaMaps {
   CUtensorMap map[MAXIN];
-  int32_t ndim;  // rank of every map: 2 + number of batch axes
-  int32_t pad[15];
+  int32_t ndim;          // rank of every map: 2 + number of batch axes
+  int32_t ext[5];        // extent of each map dimension
+  uint32_t flip[MAXIN];  // per map: batch dimensions walked backwards (bit d: coordinate ext[d] - 1 - x)
+  int32_t pad[6];
 };
 
 struct EvalTmaArgs {  // 64-byte aligned through CUtensorMap
@@ -46,12 +48,14 @@ __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
 __device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
+// try_wait suspends the thread for up to the hinted 2 us while the phase is
+// incomplete, so waiting warps do not spin on the issue slots.
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
       : "=r"(ok)
-      : "r"(bar), "r"(parity)
+      : "r"(bar), "r"(parity), "r"(2000u)
       : "memory");
   return ok != 0;
 }
@@ -225,18 +229,25 @@ __device__ __forceinline__ void tma_tile_body(const EvalPlan& p, const phcu_prog
       run_program<S, NIN, V, STASH>(prog, in, acc, st);
     }
     const bool wok = wl < nw;
+    char* o = obase + ((int64_t)rb * so_r + wl) * oes;
+    const int64_t ostep = so_r * oes;
+    switch (oes) {
+      case 4:
 #pragma unroll
-    for (int v = 0; v < V; v++) {
-      if (full || (wok && rb + v < nr)) {
-        char* o = obase + ((int64_t)(rb + v) * so_r + wl) * oes;
-        switch (oes) {
-          case 4: st_elem<S, 4>(o, acc[v]); break;
-          case 8:
-            if constexpr (sizeof(S) == 8) st_elem<S, 8>(o, acc[v]);
-            break;
-          default: st_elem<S, 1>(o, acc[v]);
+        for (int v = 0; v < V; v++)
+          if (full || (wok && rb + v < nr)) st_elem<S, 4>(o + v * ostep, acc[v]);
+        break;
+      case 8:
+        if constexpr (sizeof(S) == 8) {
+#pragma unroll
+          for (int v = 0; v < V; v++)
+            if (full || (wok && rb + v < nr)) st_elem<S, 8>(o + v * ostep, acc[v]);
         }
-      }
+        break;
+      default:
+#pragma unroll
+        for (int v = 0; v < V; v++)
+          if (full || (wok && rb + v < nr)) st_elem<S, 1>(o + v * ostep, acc[v]);
     }
   }
 }
@@ -258,10 +269,13 @@ static __device__ __noinline__ void tma_issue(const EvalTmaArgs& T, uint64_t tt,
   mbar_expect_tx(bar, nst * (two ? 2u : 1u) * TMA_BOX_BYTES);
   for (uint32_t s = 0; s < nst; s++) {
     const uint32_t dst = sb + stg * stage_bytes + s * TMA_TILE_BYTES;
-    tma_load_box(&T.maps.map[s], dst, bar, T.maps.ndim, c);
+    int32_t cs[5] = {c[0], c[1], c[2], c[3], c[4]};
+    for (int d = 2; d < 5; d++)
+      if (T.maps.flip[s] & (1u << d)) cs[d] = T.maps.ext[d] - 1 - c[d];
+    tma_load_box(&T.maps.map[s], dst, bar, T.maps.ndim, cs);
     if (two) {
-      const int32_t c2[5] = {c[0] + (int32_t)TMA_BOX_R, c[1], c[2], c[3], c[4]};
-      tma_load_box(&T.maps.map[s], dst + TMA_BOX_BYTES, bar, T.maps.ndim, c2);
+      cs[0] += (int32_t)TMA_BOX_R;
+      tma_load_box(&T.maps.map[s], dst + TMA_BOX_BYTES, bar, T.maps.ndim, cs);
     }
   }
 }

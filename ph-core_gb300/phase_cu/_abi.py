@@ -32,7 +32,7 @@ ST_OVERFLOW, ST_DIVZERO, ST_ARGUMENT, ST_TIMEOUT, ST_OOB = 1, 2, 4, 8, 16
 UOP_POS, UOP_NEG, UOP_NOT = 0, 1, 2
 RED_SUM, RED_MAX, RED_MIN, RED_ARGMAX, RED_ARGMIN = 0, 1, 2, 3, 4
 
-I_LD, I_ST0, I_ST1, I_CVT, I_NEG, I_NOT, I_POS = 64, 65, 66, 67, 68, 69, 70
+I_LD, I_ST0, I_ST1, I_CVT, I_NEG, I_NOT, I_POS, I_SEL = 64, 65, 66, 67, 68, 69, 70, 71
 SRC_IMM, SRC_S0, SRC_S1 = 8, 9, 10
 
 TASK_EVAL, TASK_REDUCE = 0, 1

@@ -465,9 +465,25 @@ class _Indexable:
 
     # ------------------------------------------------------------ compare
     def equals(self, other):
+        """MultiIndexable#equals? with == (multi_indexable.cr:871-879): the
+        elementwise comparison and the all-reduction run on the device; one
+        Int32 comes back."""
         if self.shape != other.shape:
             return False
-        return bool(np.array_equal(self.to_narr(), other.to_narr()))
+        if self.size == 0:
+            return True
+        same = self.eq(other)
+        flags = CuNArray.empty(self._shape, A.I32)
+        P = A.Program()
+        P.n_instr = 2
+        P.out_type = A.I32
+        for i, (op, t, imm) in enumerate(((A.I_LD, A.BOOL, 0), (A.I_CVT, A.BOOL, A.I32))):
+            c = P.code[i]
+            c.op, c.src, c.type, c.btype, c.flags = op, 0, t, t, 0
+            c.imm.i = imm
+        ins = (A.View * 1)(same._cview())
+        A.check(lib().phcu_eval(ctypes.byref(P), ins, 1, ctypes.byref(flags._view())), "phcu_eval")
+        return flags.min() == 1
 
     def __eq__(self, other):
         """MultiIndexable#== (multi_indexable.cr:74-84): same type, shape and elements."""
@@ -768,7 +784,10 @@ class CuNArray(_Indexable):
         if not isinstance(key, tuple):
             key = (key,)
         if len(key) == 1 and isinstance(key[0], _Indexable) and key[0].dtype == A.BOOL:
-            return self.set_mask(key[0], value)
+            # NArray#[]=(mask, value) (n_array.cr:510-551)
+            if key[0].shape != self._shape:
+                raise DimensionError("Cannot perform masking: mask shape does not match array shape.")
+            return _masked_write(self, key[0], value)
         self.set_chunk(*key, value)
 
     def set_element(self, coord, value):
@@ -781,20 +800,15 @@ class CuNArray(_Indexable):
         _write_region(self, reg, value)
 
     def set_mask(self, mask, value):
-        """MultiWritable#set_mask (multi_writable.cr:127-172): masked write,
-        evaluated as one select kernel: out = mask ? value : self."""
-        if mask.shape != self._shape:
-            raise ShapeError("Cannot perform masking: mask shape %r does not match array shape %r."
-                             % (mask.shape, self._shape))
+        """MultiWritable#set_mask (multi_writable.cr:155-172): writes value (a
+        scalar or a same-shaped MultiIndexable) where mask is true."""
         if isinstance(value, _Indexable) and value.shape != self._shape:
             raise ShapeError("Cannot perform masking: source shape %r does not match array shape %r."
                              % (value.shape, self._shape))
-        m = mask.to_narr()
-        cur = self.to_narr()
-        v = value.to_narr() if isinstance(value, _Indexable) else value
-        new = np.where(m, v, cur).astype(_NP[self.dtype])
-        A.check(lib().phcu_upload(self._buf.ptr, new.ctypes.data, new.nbytes), "phcu_upload")
-        A.call("phcu_sync")
+        if mask.shape != self._shape:
+            raise ShapeError("Cannot perform masking: mask shape %r does not match array shape %r."
+                             % (mask.shape, self._shape))
+        _masked_write(self, mask, value)
 
     def mutable_view(self, *region):
         """MultiIndexable::Mutable#mutable_view (mutable.cr:6-12)."""
@@ -929,6 +943,34 @@ class CuView(_Indexable):
         return self.to_cu().to_narr()
 
 
+def _masked_write(self, mask, value):
+    """One in-place select kernel over a writable target (an array or a
+    mutable view): self = mask ? value : self.  Program: S0 = IN0 (the mask);
+    ACC = IN2 (self); ACC = S0 ? B : ACC with B the source view IN1 or an
+    immediate."""
+    if isinstance(value, CuProcView):
+        value = value.to_cu()
+    src = value._cview() if isinstance(value, _Indexable) else None
+    if src is not None and value.dtype != self.dtype:
+        raise TypeError("masked write of a %s source into a %s array" % (np_dtype(value.dtype), np_dtype(self.dtype)))
+    me = self._cview()
+    ins = (A.View * 3)()
+    ins[0] = mask._cview()
+    ins[1] = src if src is not None else me
+    ins[2] = me
+    P = A.Program()
+    P.n_instr = 4
+    P.out_type = self.dtype
+    code = [(A.I_LD, 0, A.BOOL, A.BOOL, 0), (A.I_ST0, 0, A.BOOL, 0, 0), (A.I_LD, 2, self.dtype, self.dtype, 0),
+            (A.I_SEL, 1, self.dtype, self.dtype, 0) if src is not None else
+            (A.I_SEL, A.SRC_IMM, self.dtype, self.dtype, _slot_bits(_cast_scalar(value, self.dtype), self.dtype))]
+    for i, (op, sr, t, bt, imm) in enumerate(code):
+        c = P.code[i]
+        c.op, c.src, c.type, c.btype, c.flags = op, sr, t, bt, 0
+        c.imm.i = int(imm) if imm < 2 ** 63 else int(imm) - 2 ** 64
+    A.check(lib().phcu_eval(ctypes.byref(P), ins, 3, ctypes.byref(me)), "phcu_eval")
+
+
 class CuMutableView(CuView):
     """Writable view (src/mutable_view.cr): writes land in the source buffer."""
 
@@ -955,7 +997,11 @@ class CuMutableView(CuView):
     def __setitem__(self, key, value):
         if not isinstance(key, tuple):
             key = (key,)
+        if len(key) == 1 and isinstance(key[0], _Indexable) and key[0].dtype == A.BOOL:
+            return self.set_mask(key[0], value)  # MultiWritable#[]=(mask, value) (multi_writable.cr:127-129)
         self.set_chunk(*key, value)
+
+    set_mask = CuNArray.set_mask
 
 
 # ============================================================= CuProcView

@@ -111,7 +111,7 @@ def kats():
         {"literal": [I(-2), Rg(-1, 0)], "scalar": 6, "expected": [[6, 6, 6], [3, 4, 5]]},
         {"literal": [Rg(0, 0, x=True), Rg(0, 0, x=True)], "scalar": 6, "expected": stock},
     ]
-    k["narray_ops"] = {  # spec/n_array_spec.cr:317-322, 444-466, 505-509
+    k["narray_ops"] = {  # spec/n_array_spec.cr:297-333 (masks), 317-322, 444-466, 505-509
         "stock": stock,
         "plus_10": [[10, 11, 12], [13, 14, 15]],
         "pow_2": [[0, 1, 4], [9, 16, 25]],

@@ -38,6 +38,13 @@ def test_permuted_gathers(cu, ora, dt):
         x = _data(rng, shape, dt)
         _, v, ov = _perm(cu, ora, x, order)
         assert np.array_equal(v.to_narr(), ora.gather(ov)), (shape, order)
+    # a reversed batch axis (the tensor map walks it forwards from its last element)
+    x = _data(rng, [80, 72, 136], dt)
+    X = cu.CuNArray.from_numpy(x)
+    lits = [cu.R(None, None, -1), slice(None), slice(None)]
+    v = X.view(*lits).permute(2, 0, 1)
+    ov = ora.ViewOperand(x, [("region", lits), ("permute", [2, 0, 1])])
+    assert np.array_equal(v.to_narr(), ora.gather(ov))
     # a region whose first element is not 16-byte aligned
     x = _data(rng, [70, 66, 40], dt)
     X = cu.CuNArray.from_numpy(x)
@@ -96,12 +103,13 @@ def test_permuted_scatter(cu, ora):
         a = _data(rng, shape, np.int32)
         _, av, oa = _perm(cu, ora, a, order)
         out_shape = av.shape
-        c = np.zeros(out_shape, np.int32)
-        C = cu.CuNArray.from_numpy(c)
-        lits = [slice(None)] * len(out_shape)
-        lits[0] = cu.R(None, None, -1)
-        M = C.mutable_view(*lits)
-        M[tuple(slice(None) for _ in out_shape)] = av
-        od = ora.ViewOperand(c, [("region", lits)])
-        ora.scatter(od, oa)
-        assert np.array_equal(C.to_narr(), od.arr), (shape, order)
+        for rev in (0, 1):  # reversing output axis 0 (the R axis here) or 1 (a batch axis)
+            c = np.zeros(out_shape, np.int32)
+            C = cu.CuNArray.from_numpy(c)
+            lits = [slice(None)] * len(out_shape)
+            lits[rev] = cu.R(None, None, -1)
+            M = C.mutable_view(*lits)
+            M[tuple(slice(None) for _ in out_shape)] = av
+            od = ora.ViewOperand(c, [("region", lits)])
+            ora.scatter(od, oa)
+            assert np.array_equal(C.to_narr(), od.arr), (shape, order, rev)

@@ -167,6 +167,17 @@ def test_narray_ops(ora, kats):
     assert ora.reduce(ora.RED_MAX, b) == r["max_narr2"]
 
 
+def test_mask_writes(ora, kats):
+    """spec/n_array_spec.cr:297-333: narr[mask] = 6 and narr[mask] = stock + 10."""
+    k = kats["narray_ops"]
+    stock = np.array(k["stock"], dtype=np.int32)
+    mask = np.array(k["mask"], dtype=np.bool_)
+    assert ora.set_mask(stock.copy(), mask, 6).tolist() == k["mask_scalar_6"]
+    assert ora.set_mask(stock.copy(), mask, stock + 10).tolist() == k["mask_src_plus_10"]
+    with pytest.raises(ora.OracleError):
+        ora.set_mask(stock.copy(), mask[:, :2], 6)
+
+
 def test_transforms(ora, kats):
     t = kats["transforms"]
     assert ora.xf_apply(ora.TF_PERMUTE, t["permute"]["coord"], pattern=t["permute"]["pattern"]) == \
