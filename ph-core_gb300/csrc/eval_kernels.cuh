@@ -25,9 +25,17 @@ constexpr int min_blocks() {
   return FAST == FAST_COPY ? 4 : 3;
 }
 
+// ROW kernels of 32-bit in-place binary operators hold little besides their
+// operands: four resident blocks (64 registers) keep more loads in flight.
+template <typename S, int FAST>
+constexpr int row_min_blocks() {
+  return (FAST == FAST_BINOP && sizeof(S) == 4) ? 4 : min_blocks<FAST>();
+}
+
 // ROW: each thread handles U grid-strided chunks of VEC elements per iteration.
 template <typename S, int NIN, int VEC, int U, bool STASH, int FAST>
-__global__ void __launch_bounds__(ROW_THREADS, min_blocks<FAST>()) eval_row_kernel(const __grid_constant__ EvalArgs A) {
+__global__ void __launch_bounds__(ROW_THREADS, row_min_blocks<S, FAST>())
+    eval_row_kernel(const __grid_constant__ EvalArgs A) {
   const uint32_t nchunks = (uint32_t)(A.plan.sp.n / VEC);
   const uint32_t nthreads = gridDim.x * blockDim.x;
   uint32_t st = 0;
