@@ -207,6 +207,21 @@ def profile_class(args):
     print("profiled %d launches of %s (%s)" % (len(jobs) * (args.warmup + args.steps), args.profile_class, dt))
 
 
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic_strided_views_512x512x256.json")
+
+
+def measured_traffic(cls):
+    """DRAM bytes per launch of one operation class, from the committed ncu
+    launch-list summary (dram__bytes_read.sum + dram__bytes_write.sum); None
+    when no summary covers the class."""
+    try:
+        with open(TRAFFIC_FILE) as f:
+            t = json.load(f)
+        return t["classes"].get(cls), os.path.relpath(TRAFFIC_FILE, ROOT)
+    except (OSError, ValueError, KeyError):
+        return None, None
+
+
 def _device_timed(args, cu, A, lib, arrays, dev, jobs, run_job, step_bytes):
     n = int(np.prod(SHAPE))
 
@@ -274,10 +289,11 @@ def _device_timed(args, cu, A, lib, arrays, dev, jobs, run_job, step_bytes):
     dom_ms_per_launch = dom[1]["ms"] / dom[1]["launches"]
     dom_bytes_per_launch = dom[1]["bytes"] / dom[1]["launches"]
     achieved = dom_bytes_per_launch / (dom_ms_per_launch * 1e-3) / 1e9
+    traffic, traffic_src = measured_traffic(dom[0])
     roofline = {"bound": "hbm", "kernel": dom[0], "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                 "bytes_per_launch": int(dom_bytes_per_launch), "ms_per_launch": round(dom_ms_per_launch, 4),
-                "traffic": None, "step_frac": round(value / world / peak, 4),
+                "traffic": traffic, "traffic_source": traffic_src, "step_frac": round(value / world / peak, 4),
                 "per_class_gbs": {k: round(v["gbs"], 1) for k, v in per_class.items()}}
 
     # ------------------------------------------------------------ e2e
