@@ -430,6 +430,43 @@ def set_mask(arr, mask, value):
     return arr
 
 
+def tile(src, counts):
+    """NArray.tile (n_array.cr:242-252 with TilingLexIterator,
+    multi_indexable/tiling_lex_iterator.cr): the output walks its coordinates
+    in lexicographic order and element c takes source element c mod shape.
+    A Python loop for small cases."""
+    src = np.asarray(src)
+    shape = [n * int(c) for n, c in zip(src.shape, counts)]
+    out = np.empty(shape, dtype=src.dtype)
+    for coord in np.ndindex(*shape):
+        out[coord] = src[tuple(c % n for c, n in zip(coord, src.shape))]
+    return out
+
+
+def concatenate(narrs, axis=0):
+    """NArray.concatenate_to_slice (n_array.cr:726-749): for each chunk of the
+    axes before `axis`, the next shape[axis] * stride[axis] elements of every
+    operand in turn, each read in lexicographic order."""
+    narrs = [np.asarray(n) for n in narrs]
+    first = narrs[0]
+    for n in narrs:
+        if n.ndim != first.ndim or any(a != b for i, (a, b) in enumerate(zip(first.shape, n.shape)) if i != axis):
+            raise OracleError(ERR_DIM, "concatenate")
+    shape = list(first.shape)
+    shape[axis] = sum(n.shape[axis] for n in narrs)
+    partial = int(np.prod(first.shape[axis + 1:], dtype=np.int64))
+    num_chunks = int(np.prod(shape[:axis], dtype=np.int64))
+    flats = [n.reshape(-1) for n in narrs]
+    pos = [0] * len(narrs)
+    values = []
+    for _ in range(num_chunks):
+        for i, n in enumerate(narrs):
+            size = n.shape[axis] * partial
+            values.extend(flats[i][pos[i]:pos[i] + size].tolist())
+            pos[i] += size
+    return np.array(values, dtype=first.dtype).reshape(shape)
+
+
 def result_dtype(op, ta, tb):
     t = ctypes.c_int32()
     _chk(lib().ora_result_dtype(op, ta, tb, ctypes.byref(t)), "result_dtype")

@@ -738,6 +738,91 @@ class CuNArray(_Indexable):
         _copy_into(out._view(), self._view())
         return out
 
+    @classmethod
+    def tile(cls, source, counts):
+        """NArray.tile (n_array.cr:242-252): repeats source counts[i] times along
+        axis i.  One strided copy: the output seen as [c0, s0, c1, s1, ...]
+        receives the source read with stride 0 along every c axis (split into
+        several copies when that view would exceed the device's rank limit)."""
+        if isinstance(source, CuProcView):
+            source = source.to_cu()
+        sshape = list(source.shape)
+        counts = [int(c) for c in counts]
+        if len(counts) < len(sshape):
+            raise IndexError("tile: %d counts for a %d-dimensional source" % (len(counts), len(sshape)))
+        if any(c < 0 for c in counts[:len(sshape)]):
+            raise ValueError("tile: negative count")
+        shape = [n * c for n, c in zip(sshape, counts)]
+        out = cls(shape, source.dtype)
+        if shape_to_size(shape) == 0:
+            return out
+        sbuf, soff, _, sst = source._desc()
+        ost = _row_major(shape)
+        R = len(sshape)
+        # leading axes that a rank-8 descriptor cannot pair (lead + 2 (R - lead) <= 8) are walked on the host
+        lead = max(0, 2 * R - A.MAX_RANK)
+        for prefix in np.ndindex(*counts[:lead]) if lead else [()]:
+            dshape, dst, sshape2, sst2 = [], [], [], []
+            doff = 0
+            for i in range(R):
+                if i < lead:
+                    doff += prefix[i] * sshape[i] * ost[i]
+                    dshape.append(sshape[i])
+                    dst.append(ost[i])
+                    sshape2.append(sshape[i])
+                    sst2.append(sst[i])
+                else:
+                    dshape += [counts[i], sshape[i]]
+                    dst += [sshape[i] * ost[i], ost[i]]
+                    sshape2 += [counts[i], sshape[i]]
+                    sst2 += [0, sst[i]]
+            _copy_into(_make_view(out._buf, out.dtype, doff, dshape, dst),
+                       _make_view(sbuf, source.dtype, soff, sshape2, sst2))
+        return out
+
+    @classmethod
+    def concatenate(cls, *narrs, axis=0):
+        """NArray.concatenate (n_array.cr:719-749): one strided copy of each
+        operand into its slab of the output along `axis`."""
+        if len(narrs) == 1 and isinstance(narrs[0], (list, tuple)):
+            narrs = tuple(narrs[0])
+        narrs = [n.to_cu() if isinstance(n, CuProcView) else n for n in narrs]
+        first = narrs[0]
+        rank = first.dimensions
+        ax = axis + rank if axis < 0 else axis
+        for n in narrs[1:]:
+            if n.dimensions != rank or any(a != b for i, (a, b) in enumerate(zip(first.shape, n.shape)) if i != ax):
+                raise DimensionError("Cannot concatenate these arrays along axis %d: shapes do not match" % axis)
+            if n.dtype != first.dtype:
+                raise TypeError("Cannot concatenate arrays of different element types")
+        if not 0 <= ax < rank:
+            raise IndexError("axis %d is not present in a %d-dimensional MultiIndexable" % (axis, rank))
+        shape = list(first.shape)
+        shape[ax] = sum(n.shape[ax] for n in narrs)
+        out = cls(shape, first.dtype)
+        ost = _row_major(shape)
+        pos = 0
+        for n in narrs:
+            k = n.shape[ax]
+            if k and n.size:
+                sub = list(shape)
+                sub[ax] = k
+                _copy_into(_make_view(out._buf, out.dtype, pos * ost[ax], sub, ost), n._cview())
+            pos += k
+        return out
+
+    def push(self, *others, axis=0):
+        """NArray#push / #<< (n_array.cr:682-712): appends others along axis 0
+        in place (the buffer is replaced by the concatenation)."""
+        if axis != 0:
+            raise ValueError("push appends along axis 0 only")
+        cat = CuNArray.concatenate(self, *others, axis=0)
+        self._buf, self._shape = cat._buf, cat._shape
+        return self
+
+    def __lshift__(self, other):
+        return self.push(other)
+
     # ------------------------------------------------------------- layout
     def _desc(self):
         return self._buf, 0, list(self._shape), _row_major(self._shape)
