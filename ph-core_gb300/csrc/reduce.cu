@@ -51,6 +51,34 @@ __global__ void __launch_bounds__(256) reduce_group4_kernel(const __grid_constan
   if (st) atomicOr(a.status, st);
 }
 
+// GROUP with 16-byte loads along the reduced axis (NO outputs per group).
+template <typename T, int KIND, int G, int NO>
+__global__ void __launch_bounds__(256) reduce_group_vec_kernel(const __grid_constant__ RedArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int glane = lane & (G - 1);
+  const int groups_per_block = blockDim.x / G;
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+  uint32_t st = 0;
+  const int64_t og = (a.O + NO - 1) / NO;
+  const int64_t nwork = og * a.S;
+  for (int64_t w = (int64_t)blockIdx.x * groups_per_block + threadIdx.x / G; w < nwork;
+       w += (int64_t)gridDim.x * groups_per_block)
+    group_vec<T, KIND, G, NO>(a, (w % og) * NO, w / og, glane, gmask, st);
+  if (st) atomicOr(a.status, st);
+}
+
+// COLUMN with 16-byte loads across 16 / sizeof(T) consecutive outputs.
+template <typename T, int KIND>
+__global__ void __launch_bounds__(256) reduce_column_vec_kernel(const __grid_constant__ RedArgs a) {
+  constexpr int VN = 16 / sizeof(T);
+  uint32_t st = 0;
+  const int64_t ov = a.O / VN;
+  const int64_t nwork = ov * a.S;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < nwork; w += (int64_t)gridDim.x * blockDim.x)
+    column_vec<T, KIND>(a, (w % ov) * VN, w / ov, st);
+  if (st) atomicOr(a.status, st);
+}
+
 template <typename T, int KIND>
 __global__ void __launch_bounds__(256) reduce_column_kernel(const __grid_constant__ RedArgs a) {
   uint32_t st = 0;
@@ -81,14 +109,32 @@ template <typename T, int KIND>
 static int32_t launch_typed(const RedArgs& a, const RedShape& sh) {
   Context& c = ctx();
   const int threads = 256;
+  constexpr int VN = 16 / sizeof(T);
   // four outputs per group when the reduced axis is short and outputs are many
-  const bool four = sh.mode == 0 && a.K <= 8 * sh.G && a.O >= 4096;
-  int64_t work_threads = (sh.mode == 0) ? (four ? (a.O + 3) / 4 : a.O) * a.S * sh.G : a.O * a.S;
+  const bool four = sh.mode == 0 && a.K <= (sh.vec ? 2 * VN : 8) * sh.G && a.O >= 4096;
+  int64_t work_threads = (sh.mode == 0) ? (four ? (a.O + 3) / 4 : a.O) * a.S * sh.G
+                                        : (sh.vec ? a.O / VN : a.O) * a.S;
   int64_t blocks = (work_threads + threads - 1) / threads;
   int64_t cap = (int64_t)c.sm_count * 8 * 4;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
-  if (four) {
+  if (sh.vec && sh.mode == 1) {
+    reduce_column_vec_kernel<T, KIND><<<(unsigned)blocks, threads, 0, c.stream>>>(a);
+  } else if (sh.vec && four) {
+    switch (sh.G) {
+      case 32: reduce_group_vec_kernel<T, KIND, 32, 4><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      case 16: reduce_group_vec_kernel<T, KIND, 16, 4><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      case 8: reduce_group_vec_kernel<T, KIND, 8, 4><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      default: reduce_group_vec_kernel<T, KIND, 4, 4><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+    }
+  } else if (sh.vec) {
+    switch (sh.G) {
+      case 32: reduce_group_vec_kernel<T, KIND, 32, 1><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      case 16: reduce_group_vec_kernel<T, KIND, 16, 1><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      case 8: reduce_group_vec_kernel<T, KIND, 8, 1><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      default: reduce_group_vec_kernel<T, KIND, 4, 1><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+    }
+  } else if (four) {
     switch (sh.G) {
       case 32: reduce_group4_kernel<T, KIND, 32><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
       case 16: reduce_group4_kernel<T, KIND, 16><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
@@ -137,6 +183,7 @@ int32_t launch_reduce_plan(const RedArgs& a, int mode, int G) {
   RedShape sh;
   sh.mode = mode;
   sh.G = G;
+  sh.vec = 0;  // the batched executor's plans replay with element loads
   return launch_reduce(a, sh);
 }
 
@@ -258,22 +305,42 @@ int32_t plan_reduce(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_
     mode = 1;
   } else {
     mode = 0;
-    int64_t per = K / 4;
+  }
+  // 16-byte loads: every output row (and, for COLUMN, every reduced step) must
+  // start 16-byte aligned; GROUP also needs the reduced axis to be one axis of
+  // unit stride, COLUMN a unit-stride innermost kept axis whose length the
+  // vector divides.
+  const int es = dtype_size(t);
+  const int VN = 16 / es;
+  bool vec = ((uintptr_t)a.in % 16) == 0;
+  for (int i = 0; i < orank - (mode == 1 ? 1 : 0); i++) vec = vec && (ost[i] * es) % 16 == 0;
+  if (mode == 0) {
+    vec = vec && krank == 1 && kst[0] == 1 && K >= VN;
+  } else {
+    vec = vec && ost[orank - 1] == 1 && osh[orank - 1] % VN == 0;
+    for (int i = 0; i < krank; i++) vec = vec && (kst[i] * es) % 16 == 0;
+  }
+  if (mode == 0) {
+    // lanes per output: at least 4 elements (4 vectors) per lane, so short
+    // rows spend their time loading rather than combining across lanes
+    const int64_t per = vec ? K / (4 * VN) : K / 4;
     while (G > 4 && G > per) G >>= 1;
   }
   int64_t S = 1;
-  const int64_t tpw = (mode == 0) ? G : 1;
-  if (O * tpw < target) {
-    S = (target + O * tpw - 1) / (O * tpw);
+  const int64_t units = (mode == 0) ? O * G : O;
+  if (units < target) {
+    S = (target + units - 1) / units;
     int64_t min_chunk = (mode == 0) ? (int64_t)G * 16 : 32;
     int64_t smax = (K + min_chunk - 1) / min_chunk;
     if (S > smax) S = smax;
     if (S < 1) S = 1;
   }
   a.chunk = (K + S - 1) / S;
+  if (vec && mode == 0) a.chunk = (a.chunk + VN - 1) / VN * VN;  // splits start on whole vectors
   a.S = (K + a.chunk - 1) / a.chunk;
   shape->mode = mode;
   shape->G = G;
+  shape->vec = vec ? 1 : 0;
   return PHCU_OK;
 }
 

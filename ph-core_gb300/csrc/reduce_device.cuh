@@ -198,6 +198,18 @@ __device__ __forceinline__ T ld(const char* p) {
   return *(const T*)p;
 }
 
+// reinterpretations of loaded 32- / 64-bit words as T
+template <typename T>
+__device__ __forceinline__ T word32_as(uint32_t u) {
+  if constexpr (std::is_same<T, float>::value) return __uint_as_float(u);
+  else return (T)(int32_t)u;
+}
+template <typename T>
+__device__ __forceinline__ T word64_as(unsigned long long u) {
+  if constexpr (std::is_same<T, double>::value) return __longlong_as_double((long long)u);
+  else return (T)(long long)u;
+}
+
 __device__ __forceinline__ void store_final(const RedArgs& a, int64_t o, double v, long long vi, bool is_int_sum, long long isum,
                             long long index, uint32_t& st) {
   char* p = a.out + o * dtype_size(a.out_dtype);
@@ -370,6 +382,154 @@ __device__ __forceinline__ void group_multi(const RedArgs& a, int64_t o0, int64_
     }
     if (glane == 0 && o0 + q < a.O) finish<T, KIND>(a, o0 + q, split, sacc[q], eacc[q], st);
   }
+}
+
+// 16-byte loads of VN = 16 / sizeof(T) consecutive elements.
+template <typename T>
+__device__ __forceinline__ void ld16(const char* p, T* x) {
+  if constexpr (sizeof(T) == 4) {
+    const uint4 v = __ldg((const uint4*)p);
+    x[0] = word32_as<T>(v.x);
+    x[1] = word32_as<T>(v.y);
+    x[2] = word32_as<T>(v.z);
+    x[3] = word32_as<T>(v.w);
+  } else {
+    const ulonglong2 v = __ldg((const ulonglong2*)p);
+    x[0] = word64_as<T>(v.x);
+    x[1] = word64_as<T>(v.y);
+  }
+}
+
+// GROUP with 16-byte loads along a contiguous reduced axis: lane l of a group
+// of G reads vectors l, l + G, l + 2G, ... of each of NO outputs (elements of
+// one accumulator arrive in increasing k), then the < VN elements past the last
+// whole vector one per lane.  Requires: the reduced axis is one axis of unit
+// stride; every output row and every split starts 16-byte aligned.
+template <typename T, int KIND, int G, int NO>
+__device__ __forceinline__ void group_vec(const RedArgs& a, int64_t o0, int64_t split, int glane, unsigned gmask,
+                                          uint32_t& st) {
+  constexpr int VN = 16 / sizeof(T);
+  constexpr int U = NO == 1 ? 4 : 1;  // vectors in flight per output and lane
+  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
+  const int64_t k0 = split * a.chunk;
+  const int64_t k1 = min(a.K, k0 + a.chunk);
+  const int64_t kv1 = k0 + (k1 - k0) / VN * VN;  // end of the whole vectors
+  const char* base[NO];
+  SumAcc<T> sacc[NO];
+  ExtAcc<T> eacc[NO];
+#pragma unroll
+  for (int q = 0; q < NO; q++) {
+    const int64_t o = min(o0 + q, a.O - 1);  // past the end: repeat the last output (not stored)
+    base[q] = a.in + out_offset(a, (uint32_t)o) * (int64_t)sizeof(T);
+    sacc[q].init();
+    eacc[q].init();
+  }
+  int64_t k = k0 + (int64_t)glane * VN;
+  for (; k + (int64_t)(U - 1) * G * VN + VN <= kv1; k += (int64_t)U * G * VN) {
+    T x[NO][U][VN];
+#pragma unroll
+    for (int q = 0; q < NO; q++)
+#pragma unroll
+      for (int u = 0; u < U; u++) ld16<T>(base[q] + (k + (int64_t)u * G * VN) * (int64_t)sizeof(T), x[q][u]);
+#pragma unroll
+    for (int q = 0; q < NO; q++)
+#pragma unroll
+      for (int u = 0; u < U; u++)
+#pragma unroll
+        for (int e = 0; e < VN; e++) {
+          if (KIND == RK_SUM) sacc[q].add(x[q][u][e]);
+          else eacc[q].add(x[q][u][e], k + (int64_t)u * G * VN + e, is_max);
+        }
+  }
+  for (; k + VN <= kv1; k += (int64_t)G * VN) {
+#pragma unroll
+    for (int q = 0; q < NO; q++) {
+      T x[VN];
+      ld16<T>(base[q] + k * (int64_t)sizeof(T), x);
+#pragma unroll
+      for (int e = 0; e < VN; e++) {
+        if (KIND == RK_SUM) sacc[q].add(x[e]);
+        else eacc[q].add(x[e], k + e, is_max);
+      }
+    }
+  }
+  const int64_t kt = kv1 + glane;  // the tail: one element per lane
+  if (kt < k1) {
+#pragma unroll
+    for (int q = 0; q < NO; q++) {
+      const T x = ld<T>(base[q] + kt * (int64_t)sizeof(T));
+      if (KIND == RK_SUM) sacc[q].add(x);
+      else eacc[q].add(x, kt, is_max);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NO; q++) {
+#pragma unroll
+    for (int d = G / 2; d >= 1; d >>= 1) {
+      if (KIND == RK_SUM) sacc[q].shfl(d, gmask, G);
+      else eacc[q].shfl(d, gmask, G, is_max);
+    }
+    if (glane == 0 && o0 + q < a.O) finish<T, KIND>(a, o0 + q, split, sacc[q], eacc[q], st);
+  }
+}
+
+// COLUMN with 16-byte loads across outputs: one thread reduces VN consecutive
+// outputs o0 .. o0 + VN - 1, which are consecutive in memory (the innermost
+// kept axis has unit stride and a length divisible by VN), four reduced
+// positions in flight.  Requires every output row start and every reduced
+// stride to be 16-byte aligned.
+template <typename T, int KIND>
+__device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t split, uint32_t& st) {
+  constexpr int VN = 16 / sizeof(T);
+  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
+  const int64_t k0 = split * a.chunk;
+  const int64_t k1 = min(a.K, k0 + a.chunk);
+  const char* base = a.in + out_offset(a, (uint32_t)o0) * (int64_t)sizeof(T);
+  SumAcc<T> sacc[VN];
+  ExtAcc<T> eacc[VN];
+#pragma unroll
+  for (int e = 0; e < VN; e++) {
+    sacc[e].init();
+    eacc[e].init();
+  }
+  int64_t k = k0;
+  if (a.krank == 1) {
+    const int64_t ks = a.kinner * (int64_t)sizeof(T);
+    const char* p = base + k0 * ks;
+    for (; k + 3 < k1; k += 4, p += 4 * ks) {
+      T x[4][VN];
+#pragma unroll
+      for (int j = 0; j < 4; j++) ld16<T>(p + j * ks, x[j]);
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+#pragma unroll
+        for (int e = 0; e < VN; e++) {
+          if (KIND == RK_SUM) sacc[e].add(x[j][e]);
+          else eacc[e].add(x[j][e], k + j, is_max);
+        }
+    }
+    for (; k < k1; k++, p += ks) {
+      T x[VN];
+      ld16<T>(p, x);
+#pragma unroll
+      for (int e = 0; e < VN; e++) {
+        if (KIND == RK_SUM) sacc[e].add(x[e]);
+        else eacc[e].add(x[e], k, is_max);
+      }
+    }
+  } else {
+    for (; k < k1; k++) {
+      T x[VN];
+      ld16<T>(base + k_offset(a, (uint32_t)k) * (int64_t)sizeof(T), x);
+#pragma unroll
+      for (int e = 0; e < VN; e++) {
+        if (KIND == RK_SUM) sacc[e].add(x[e]);
+        else eacc[e].add(x[e], k, is_max);
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < VN; e++) finish<T, KIND>(a, o0 + e, split, sacc[e], eacc[e], st);
 }
 
 // COLUMN: one thread reduces elements [k0, k1) of output o.
@@ -570,6 +730,7 @@ __device__ __forceinline__ void combine_block(const RedArgs& a, int64_t o, Combi
 struct RedShape {
   int mode;  // 0 = GROUP, 1 = COLUMN
   int G;
+  int vec;   // 1: 16-byte loads (group_vec / column_vec)
 };
 int32_t plan_reduce(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_view_t* out, int64_t target_threads,
                     RedArgs* a, RedShape* shape, bool* trivial, bool* empty_sum);
