@@ -738,6 +738,29 @@ class CuNArray(_Indexable):
         _copy_into(out._view(), self._view())
         return out
 
+    # ------------------------------------------------------- serialisation
+    def to_json(self):
+        """NArray#to_json (n_array.cr:807-817): one bulk download."""
+        from . import serial
+        return serial.to_json(self.to_narr())
+
+    def to_yaml(self):
+        """NArray#to_yaml (n_array.cr:854-868): one bulk download."""
+        from . import serial
+        return serial.to_yaml(self.to_narr())
+
+    @classmethod
+    def from_json(cls, text, dtype):
+        """NArray(T).from_json (n_array.cr:819-852): parse, then one upload."""
+        from . import serial
+        return cls.from_numpy(serial.from_json(text, _NP[dtype]))
+
+    @classmethod
+    def from_yaml(cls, text, dtype):
+        """NArray(T).from_yaml (n_array.cr:870-911): parse, then one upload."""
+        from . import serial
+        return cls.from_numpy(serial.from_yaml(text, _NP[dtype]))
+
     @classmethod
     def tile(cls, source, counts):
         """NArray.tile (n_array.cr:242-252): repeats source counts[i] times along

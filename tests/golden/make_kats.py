@@ -121,6 +121,12 @@ def kats():
         "mask_scalar_6": [[6, 1, 6], [3, 6, 5]],
         "mask_src_plus_10": [[10, 1, 12], [3, 14, 5]],
     }
+    k["serialization"] = {  # spec/n_array_spec.cr:520-557
+        "stock_json": '{"shape":[2,3],"elements":[0,1,2,3,4,5]}',
+        "empty_json": '{"shape":[0],"elements":[]}',
+        "stock_yaml": "---\nshape: [2, 3]\nelements: [0, 1, 2, 3, 4, 5]\n",
+        "empty_yaml": "---\nshape: [0]\nelements: []\n",
+    }
     # README.md:36-61: narr + narr2, narr * narr2, argmax idiom
     k["readme"] = {"narr": [[1, 0, 0], [0, 1, 0]], "narr2": [[0, 1, 2], [10, 11, 12]],
                    "sum": [[1, 1, 2], [10, 12, 12]], "prod": [[0, 0, 0], [0, 11, 0]],

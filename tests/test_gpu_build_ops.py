@@ -50,3 +50,18 @@ def test_concatenate_and_push(cu, ora):
     assert np.array_equal(A_.to_narr(), ora.concatenate([a, b[::-1], b], 0))
     with pytest.raises(cu.DimensionError):
         cu.CuNArray.concatenate(cu.CuNArray.from_numpy(a), cu.CuNArray.from_numpy(b), axis=1)
+
+
+def test_serialisation_on_device_arrays(cu, kats):
+    """spec/n_array_spec.cr:520-557 through device arrays (one download / upload)."""
+    k = kats["serialization"]
+    stock = cu.CuNArray.from_numpy(np.array(kats["narray_ops"]["stock"], np.int32))
+    assert stock.to_json() == k["stock_json"]
+    assert stock.to_yaml() == k["stock_yaml"]
+    assert cu.CuNArray.from_json(k["stock_json"], cu.Int32) == stock
+    assert cu.CuNArray.from_yaml(k["stock_yaml"], cu.Int32) == stock
+    assert cu.CuNArray.fill([0], 0).to_json() == k["empty_json"]
+    assert cu.CuNArray.from_yaml(k["empty_yaml"], cu.Int32).shape == [0]
+    x = np.random.default_rng(3).standard_normal([4, 5]).astype(np.float32)
+    X = cu.CuNArray.from_numpy(x)
+    assert np.array_equal(cu.CuNArray.from_json(X.to_json(), cu.Float32).to_narr(), x)

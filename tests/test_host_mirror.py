@@ -335,3 +335,33 @@ def test_program_compiler_shapes():
     P, _ = N.compile_program(e, A.F32)
     ops = [P.code[i].op for i in range(P.n_instr)]
     assert A.I_ST0 in ops
+
+
+def test_serialisation_kats(kats):
+    """spec/n_array_spec.cr:520-557: to_json/from_json/to_yaml/from_yaml."""
+    from phase_cu import serial
+
+    k = kats["serialization"]
+    stock = np.array(kats["narray_ops"]["stock"], np.int32)
+    assert serial.to_json(stock) == k["stock_json"]
+    assert serial.to_json(np.zeros([0], np.int32)) == k["empty_json"]
+    assert serial.to_yaml(stock) == k["stock_yaml"]
+    assert serial.to_yaml(np.zeros([0], np.int32)) == k["empty_yaml"]
+    assert np.array_equal(serial.from_json(k["stock_json"], np.int32), stock)
+    assert serial.from_json(k["empty_json"], np.int32).shape == (0,)
+    assert np.array_equal(serial.from_yaml(k["stock_yaml"], np.int32), stock)
+    assert serial.from_yaml(k["empty_yaml"], np.int32).shape == (0,)
+    # round trips of the other element types, block-style YAML, and the errors
+    rng = np.random.default_rng(7)
+    for dt in (np.float32, np.float64, np.int64, np.bool_):
+        x = (rng.standard_normal([3, 4]) * 1e3).astype(dt)
+        assert np.array_equal(serial.from_json(serial.to_json(x), dt), x)
+        assert np.array_equal(serial.from_yaml(serial.to_yaml(x), dt), x)
+    assert serial.from_yaml("shape:\n- 2\nelements:\n- 1\n- 2\n", np.int32).tolist() == [1, 2]
+    with pytest.raises(serial.SerialError):
+        serial.from_json('{"shape":[2,3],"elements":[1]}', np.int32)
+    with pytest.raises(serial.SerialError):
+        serial.from_json('{"elements":[1]}', np.int32)
+    with pytest.raises(serial.SerialError):
+        serial.to_json(np.array([np.nan], np.float32))
+    assert serial.to_yaml(np.array([np.nan, np.inf], np.float32)) == "---\nshape: [2]\nelements: [.nan, .inf]\n"
