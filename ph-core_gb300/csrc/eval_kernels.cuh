@@ -33,14 +33,28 @@ constexpr int row_min_blocks() {
 }
 
 // ROW: each thread handles U grid-strided chunks of VEC elements per iteration.
+// Interpreted programs are copied to shared memory first: the interpreter
+// reads one instruction per step at a run-time index, which shared memory
+// serves with one vector load (kernel-parameter space would serialise it).
 template <typename S, int NIN, int VEC, int U, bool STASH, int FAST>
 __global__ void __launch_bounds__(ROW_THREADS, row_min_blocks<S, FAST>())
     eval_row_kernel(const __grid_constant__ EvalArgs A) {
   const uint32_t nchunks = (uint32_t)(A.plan.sp.n / VEC);
   const uint32_t nthreads = gridDim.x * blockDim.x;
   uint32_t st = 0;
-  for (uint32_t c0 = blockIdx.x * blockDim.x + threadIdx.x; c0 < nchunks; c0 += nthreads * U)
-    row_group<S, NIN, VEC, U, STASH, FAST>(A.plan, A.prog, c0, nthreads, nchunks, st);
+  if constexpr (FAST == FAST_NONE) {
+    __shared__ __align__(16) phcu_program_t s_prog;
+    static_assert(sizeof(phcu_program_t) % 8 == 0, "program copied in 8-byte words");
+    constexpr int WORDS = (int)(sizeof(phcu_program_t) / 8);
+    for (int i = threadIdx.x; i < WORDS; i += blockDim.x)
+      reinterpret_cast<uint2*>(&s_prog)[i] = reinterpret_cast<const uint2*>(&A.prog)[i];
+    __syncthreads();
+    for (uint32_t c0 = blockIdx.x * blockDim.x + threadIdx.x; c0 < nchunks; c0 += nthreads * U)
+      row_group<S, NIN, VEC, U, STASH, FAST>(A.plan, s_prog, c0, nthreads, nchunks, st);
+  } else {
+    for (uint32_t c0 = blockIdx.x * blockDim.x + threadIdx.x; c0 < nchunks; c0 += nthreads * U)
+      row_group<S, NIN, VEC, U, STASH, FAST>(A.plan, A.prog, c0, nthreads, nchunks, st);
+  }
   if (st) report_status(A.status, st);
 }
 

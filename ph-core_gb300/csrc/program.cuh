@@ -587,6 +587,25 @@ __device__ __forceinline__ void un_vec(int op, int T, S* a, uint32_t& st) {
 template <typename S, int V>
 __device__ __forceinline__ void cvt_vec(S* a, int from, int to) {
   if (from == to) return;
+  // one dispatch on the (from, to) pair, then a straight loop of that conversion
+#define PHCU_CVT(F, T_) \
+  case (F) * 8 + (T_): PHCU_LOOP a[v] = convert_slot<S>(a[v], (F), (T_)); return;
+  switch (from * 8 + to) {
+    PHCU_CVT(PHCU_BOOL, PHCU_I32) PHCU_CVT(PHCU_BOOL, PHCU_F32) PHCU_CVT(PHCU_I32, PHCU_BOOL)
+    PHCU_CVT(PHCU_I32, PHCU_F32) PHCU_CVT(PHCU_F32, PHCU_BOOL) PHCU_CVT(PHCU_F32, PHCU_I32)
+    default: break;
+  }
+  if constexpr (sizeof(S) == 8) {
+    switch (from * 8 + to) {
+      PHCU_CVT(PHCU_BOOL, PHCU_I64) PHCU_CVT(PHCU_BOOL, PHCU_F64) PHCU_CVT(PHCU_I32, PHCU_I64)
+      PHCU_CVT(PHCU_I32, PHCU_F64) PHCU_CVT(PHCU_I64, PHCU_BOOL) PHCU_CVT(PHCU_I64, PHCU_I32)
+      PHCU_CVT(PHCU_I64, PHCU_F32) PHCU_CVT(PHCU_I64, PHCU_F64) PHCU_CVT(PHCU_F32, PHCU_I64)
+      PHCU_CVT(PHCU_F32, PHCU_F64) PHCU_CVT(PHCU_F64, PHCU_BOOL) PHCU_CVT(PHCU_F64, PHCU_I32)
+      PHCU_CVT(PHCU_F64, PHCU_I64) PHCU_CVT(PHCU_F64, PHCU_F32)
+      default: break;
+    }
+  }
+#undef PHCU_CVT
   PHCU_LOOP a[v] = convert_slot<S>(a[v], from, to);
 }
 
@@ -612,8 +631,13 @@ __device__ __forceinline__ void powi_uniform(S* a, int T, int32_t e) {
 #pragma unroll
       for (int v = 0; v < V; v++) x[v] = x[v] * x[v];
     }
+    if (recip) {
 #pragma unroll
-    for (int v = 0; v < V; v++) a[v] = pf32<S>(recip ? 1.0f / r[v] : r[v]);
+      for (int v = 0; v < V; v++) a[v] = pf32<S>(1.0f / r[v]);
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; v++) a[v] = pf32<S>(r[v]);
+    }
   } else if constexpr (sizeof(S) == 8) {
     double x[V], r[V];
 #pragma unroll
@@ -631,8 +655,13 @@ __device__ __forceinline__ void powi_uniform(S* a, int T, int32_t e) {
 #pragma unroll
       for (int v = 0; v < V; v++) x[v] = x[v] * x[v];
     }
+    if (recip) {
 #pragma unroll
-    for (int v = 0; v < V; v++) a[v] = pf64(recip ? 1.0 / r[v] : r[v]);
+      for (int v = 0; v < V; v++) a[v] = pf64(1.0 / r[v]);
+    } else {
+#pragma unroll
+      for (int v = 0; v < V; v++) a[v] = pf64(r[v]);
+    }
   }
 }
 
@@ -656,6 +685,23 @@ __device__ __forceinline__ void run_binop(const phcu_program_t& P, S* a, const S
 }
 
 // ------------------------------------------------------ the interpreter
+// ACC = ACC op B on V elements in the compute type T (B already of type T, or
+// an integer exponent of a float power).
+template <typename S, int V>
+__device__ __forceinline__ void bin_dispatch(int op, int T, int bt, S* acc, const S* b, uint32_t& st) {
+  switch (T) {
+    case PHCU_F32: bin_f32<S, V>(op, bt, acc, b, st); break;
+    case PHCU_I32: bin_i32<S, V>(op, acc, b, st); break;
+    case PHCU_BOOL: bin_bool<S, V>(op, acc, b); break;
+    case PHCU_F64:
+      if constexpr (sizeof(S) == 8) bin_f64<V>(op, bt, acc, b, st);
+      break;
+    case PHCU_I64:
+      if constexpr (sizeof(S) == 8) bin_i64<V>(op, acc, b, st);
+      break;
+  }
+}
+
 // Runs the program on V elements: in[k][v] are the loaded inputs, acc[v]
 // receives the result.  STASH=false instantiations require a program without
 // ST0/ST1 and without stash operands (the host checks).
@@ -692,10 +738,16 @@ __device__ __forceinline__ void run_program(const phcu_program_t& P, const S (&i
       powi_uniform<S, V>(acc, T, P.code[pc].btype == PHCU_I32 ? (int32_t)(uint32_t)e : (int32_t)e);
       continue;
     }
+    int bt = P.code[pc].btype;
+    const bool int_exp = (op == PHCU_OP_POW) && is_float_t(T) && is_int_t(bt);
     // operand B
     S b[V];
-    if (src == PHCU_SRC_IMM) {
-      const S imm = (S)(uint64_t)P.code[pc].imm.i;
+    if (src == PHCU_SRC_IMM) {  // an immediate is converted once, then broadcast
+      S imm = (S)(uint64_t)P.code[pc].imm.i;
+      if (!int_exp && bt != T) {
+        imm = convert_slot<S>(imm, bt, T);
+        bt = T;
+      }
       PHCU_LOOP b[v] = imm;
     } else if (STASH && src == PHCU_SRC_S0) {
       PHCU_LOOP b[v] = s0[v];
@@ -713,8 +765,6 @@ __device__ __forceinline__ void run_program(const phcu_program_t& P, const S (&i
         if (src == 3) { PHCU_LOOP b[v] = in[3][v]; }
       }
     }
-    int bt = P.code[pc].btype;
-    const bool int_exp = (op == PHCU_OP_POW) && is_float_t(T) && is_int_t(bt);
     if (!int_exp && bt != T) {
       cvt_vec<S, V>(b, bt, T);
       bt = T;
@@ -736,17 +786,7 @@ __device__ __forceinline__ void run_program(const phcu_program_t& P, const S (&i
         b[v] = t;
       }
     }
-    switch (T) {
-      case PHCU_F32: bin_f32<S, V>(op, bt, acc, b, st); break;
-      case PHCU_I32: bin_i32<S, V>(op, acc, b, st); break;
-      case PHCU_BOOL: bin_bool<S, V>(op, acc, b); break;
-      case PHCU_F64:
-        if constexpr (sizeof(S) == 8) bin_f64<V>(op, bt, acc, b, st);
-        break;
-      case PHCU_I64:
-        if constexpr (sizeof(S) == 8) bin_i64<V>(op, acc, b, st);
-        break;
-    }
+    bin_dispatch<S, V>(op, T, bt, acc, b, st);
   }
 }
 
