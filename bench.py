@@ -207,6 +207,21 @@ def profile_class(args):
     print("profiled %d launches of %s (%s)" % (len(jobs) * (args.warmup + args.steps), args.profile_class, dt))
 
 
+def replica_max_ms(ms, dist, device):
+    """Replicas only: the job's time is the slowest rank's (an all-reduce MAX;
+    it also holds every rank until all have finished the timed region)."""
+    import torch
+
+    tt = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def job_gbs(step_bytes, world, ms_per_step):
+    """Whole-job throughput: every rank moves step_bytes per step."""
+    return step_bytes * world / (ms_per_step * 1e-3) / 1e9
+
+
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic_strided_views_512x512x256.json")
 
 
@@ -245,7 +260,10 @@ def _device_timed(args, cu, A, lib, arrays, dev, jobs, run_job, step_bytes):
     rank = int(os.environ.get("RANK", "0"))
     dist = None
     if world > 1:
+        import torch
         import torch.distributed as dist  # replicas only: one barrier, a max of times
+        if args.gpus > 1:
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl" if args.gpus > 1 else "gloo")
         dist.barrier()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
@@ -263,12 +281,9 @@ def _device_timed(args, cu, A, lib, arrays, dev, jobs, run_job, step_bytes):
     A.call("phcu_sync")
     clk = clocks.stop()
     if dist is not None:
-        import torch
-        tt = torch.tensor([ms], dtype=torch.float64, device="cuda" if args.gpus > 1 else "cpu")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+        ms = replica_max_ms(ms, dist, "cuda" if args.gpus > 1 else "cpu")
     ms_per_step = ms / args.steps
-    value = step_bytes * world / (ms_per_step * 1e-3) / 1e9
+    value = job_gbs(step_bytes, world, ms_per_step)
 
     # per-class kernel timing (same launches, one class at a time) for the roofline
     classes = {}
