@@ -237,6 +237,32 @@ def measured_traffic(cls):
         return None, None
 
 
+def profile_config(args):
+    """One untimed pass of a secondary workload, for ncu: c3 (the fused chain
+    over 64x128x128x64, then sum/max/argmax along every axis and the full sum)
+    or c4 (8 heat steps on 4096x4096 without a graph)."""
+    import phase_cu as cu
+    from phase_cu import _abi as A
+    from phase_cu import synth
+
+    cu.init(0)
+    lib = A.load()
+    if args.profile_config == "c3":
+        shape = [64, 128, 128, 64]
+        x, y, z = (cu.CuNArray.from_numpy(synth.lognormal_f32(shape, s)) for s in (0, 1, 2))
+        r = (x.process(lambda e: (e + 4) ** 2) * y - z).to_cu()
+        for k in range(4):
+            r.sum(axis=k), r.max(axis=k), r.argmax(axis=k)
+        r.sum()
+    else:
+        from phase_cu import stencil
+
+        hs = stencil.Heat(synth.gaussian_bumps_f32(4096, 4096, bumps=16, seed=0))
+        hs.run(8, use_graph=False)
+    A.call("phcu_sync")
+    print("profiled %s" % args.profile_config)
+
+
 def _device_timed(args, cu, A, lib, arrays, dev, jobs, run_job, step_bytes):
     n = int(np.prod(SHAPE))
 
@@ -605,9 +631,14 @@ def main():
                    help="run only one operation class (gather_permute, gather_reverse, binary_permute, "
                         "binary_reverse, scatter) for profiling")
     p.add_argument("--profile-dtype", default="f32")
+    p.add_argument("--profile-config", default=None, choices=["c3", "c4"],
+                   help="one untimed pass of the fused-chain/reduction (c3) or heat (c4) workload, for profiling")
     args = p.parse_args()
     if args.profile_class:
         profile_class(args)
+        return
+    if args.profile_config:
+        profile_config(args)
         return
     if args.impl == "reference":
         res, rank = reference_arm(args)

@@ -251,6 +251,8 @@ __device__ __forceinline__ void finish(const RedArgs& a, int64_t o, int64_t spli
       } else {
         P.v = sacc.value();
         P.i = 0;
+        if constexpr (std::is_same<T, float>::value)  // the FP32 pair too, for combine_block
+          P.i = (long long)(((unsigned long long)__float_as_uint(sacc.s) << 32) | __float_as_uint(sacc.c));
       }
     } else {
       P.v = (double)eacc.v;
@@ -400,6 +402,24 @@ __device__ __forceinline__ void ld16(const char* p, T* x) {
   }
 }
 
+// Folds VN consecutive elements (indices k0 .. k0 + VN - 1) into an extremum
+// accumulator: the vector's own first extreme (NaNs skipped, strict
+// comparison, so ties keep the lower index) is found with a 32-bit local
+// index, then offered to the accumulator once; since the accumulator only
+// holds lower indices, this equals offering the elements one by one.
+template <typename T, int VN>
+__device__ __forceinline__ void vec_extreme_into(ExtAcc<T>& acc, const T* x, int64_t k0, bool is_max) {
+  T bv = x[0];
+  int be = Lim<T>::nan(x[0]) ? -1 : 0;
+#pragma unroll
+  for (int e = 1; e < VN; e++) {
+    const bool take = !Lim<T>::nan(x[e]) && (be < 0 || (is_max ? (x[e] > bv) : (x[e] < bv)));
+    bv = take ? x[e] : bv;
+    be = take ? e : be;
+  }
+  if (be >= 0) acc.add(bv, k0 + be, is_max);
+}
+
 // GROUP with 16-byte loads along a contiguous reduced axis: lane l of a group
 // of G reads vectors l, l + G, l + 2G, ... of each of NO outputs (elements of
 // one accumulator arrive in increasing k), then the < VN elements past the last
@@ -434,22 +454,25 @@ __device__ __forceinline__ void group_vec(const RedArgs& a, int64_t o0, int64_t 
 #pragma unroll
     for (int q = 0; q < NO; q++)
 #pragma unroll
-      for (int u = 0; u < U; u++)
+      for (int u = 0; u < U; u++) {
+        if (KIND == RK_SUM) {
 #pragma unroll
-        for (int e = 0; e < VN; e++) {
-          if (KIND == RK_SUM) sacc[q].add(x[q][u][e]);
-          else eacc[q].add(x[q][u][e], k + (int64_t)u * G * VN + e, is_max);
+          for (int e = 0; e < VN; e++) sacc[q].add(x[q][u][e]);
+        } else {
+          vec_extreme_into<T, VN>(eacc[q], x[q][u], k + (int64_t)u * G * VN, is_max);
         }
+      }
   }
   for (; k + VN <= kv1; k += (int64_t)G * VN) {
 #pragma unroll
     for (int q = 0; q < NO; q++) {
       T x[VN];
       ld16<T>(base[q] + k * (int64_t)sizeof(T), x);
+      if (KIND == RK_SUM) {
 #pragma unroll
-      for (int e = 0; e < VN; e++) {
-        if (KIND == RK_SUM) sacc[q].add(x[e]);
-        else eacc[q].add(x[e], k + e, is_max);
+        for (int e = 0; e < VN; e++) sacc[q].add(x[e]);
+      } else {
+        vec_extreme_into<T, VN>(eacc[q], x, k, is_max);
       }
     }
   }
@@ -646,6 +669,37 @@ __device__ __forceinline__ void combine_block(const RedArgs& a, int64_t o, Combi
       __syncthreads();
     }
     if (t == 0) store_final(a, o, 0, 0, true, sh_i[0], 0, st);
+  } else if (KIND == RK_SUM && std::is_same<T, float>::value) {
+    // Float32 partials carry their (sum, compensation) pair: fold them as
+    // double-float values with FP32 TwoSum (FP64 throughput would make this
+    // one block the slowest part of a full reduction)
+    float* sv = reinterpret_cast<float*>(sh_v);
+    float* sc = reinterpret_cast<float*>(sh_c);
+    float s = 0.f, c = 0.f;
+    for (int64_t j = t; j < a.S; j += nt) {
+      const unsigned long long w = (unsigned long long)a.partial[j * a.O + o].i;
+      const float ps = __uint_as_float((uint32_t)(w >> 32)), pc = __uint_as_float((uint32_t)w);
+      const float u = s + ps;
+      const float bp = u - s;
+      const float e = (s - (u - bp)) + (ps - bp);
+      s = u;
+      c = (c + pc) + e;
+    }
+    sv[t] = s;
+    sc[t] = c;
+    __syncthreads();
+    for (int w = nt / 2; w >= 1; w >>= 1) {
+      if (t < w) {
+        const float x = sv[t], y = sv[t + w];
+        const float u = x + y;
+        const float bp = u - x;
+        const float e = (x - (u - bp)) + (y - bp);
+        sv[t] = u;
+        sc[t] = (sc[t] + sc[t + w]) + e;
+      }
+      __syncthreads();
+    }
+    if (t == 0) store_final(a, o, (double)sv[0] + (double)sc[0], 0, false, 0, 0, st);
   } else if (KIND == RK_SUM) {
     double s = 0.0, c = 0.0;
     for (int64_t j = t; j < a.S; j += nt) {
