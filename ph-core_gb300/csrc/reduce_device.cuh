@@ -676,15 +676,23 @@ __device__ __forceinline__ void combine_block(const RedArgs& a, int64_t o, Combi
     float* sv = reinterpret_cast<float*>(sh_v);
     float* sc = reinterpret_cast<float*>(sh_c);
     float s = 0.f, c = 0.f;
-    for (int64_t j = t; j < a.S; j += nt) {
-      const unsigned long long w = (unsigned long long)a.partial[j * a.O + o].i;
+    auto fold = [&](unsigned long long w) {
       const float ps = __uint_as_float((uint32_t)(w >> 32)), pc = __uint_as_float((uint32_t)w);
       const float u = s + ps;
       const float bp = u - s;
       const float e = (s - (u - bp)) + (ps - bp);
       s = u;
       c = (c + pc) + e;
+    };
+    int64_t j = t;
+    for (; j + 3 * nt < a.S; j += 4 * nt) {  // four loads in flight, folded in order
+      unsigned long long w[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) w[q] = (unsigned long long)a.partial[(j + q * nt) * a.O + o].i;
+#pragma unroll
+      for (int q = 0; q < 4; q++) fold(w[q]);
     }
+    for (; j < a.S; j += nt) fold((unsigned long long)a.partial[j * a.O + o].i);
     sv[t] = s;
     sc[t] = c;
     __syncthreads();

@@ -151,7 +151,10 @@ __global__ void __launch_bounds__(HEAT_BLOCK_THREADS) heat_block_kernel(const T*
       heat_ld4(src + b - HEAT_SC, up);
       heat_ld4(src + b, cv);
       heat_ld4(src + b + HEAT_SC, dn);
-      const T lft = src[b - 1], rgt = src[b + 4];
+      // the neighbouring lanes' end cells; lanes 0 and 31 hold the tile's outer
+      // columns, whose results are never exact, so their wrapped values do not matter
+      const T lft = __shfl_up_sync(0xffffffffu, cv[3], 1);
+      const T rgt = __shfl_down_sync(0xffffffffu, cv[0], 1);
 #pragma unroll
       for (int e = 0; e < 4; e++) {
         const T left = e == 0 ? lft : cv[e - 1];
