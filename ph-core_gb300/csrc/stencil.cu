@@ -198,11 +198,8 @@ static void enqueue_heat(const T* u, T* out, int64_t n, int64_t m, T coef, cudaS
 template <typename T>
 static void enqueue_heat_block(const T* u, T* out, int64_t n, int64_t m, T coef, int ksteps, cudaStream_t s) {
   const size_t smem = 2 * (size_t)HEAT_SR * HEAT_SC * sizeof(T);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(heat_block_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr = true;
-  }
+  // per launch: the attribute belongs to the current device's context
+  cudaFuncSetAttribute(heat_block_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 grid((unsigned)((m + HEAT_TC - 1) / HEAT_TC), (unsigned)((n + HEAT_TR - 1) / HEAT_TR));
   heat_block_kernel<T><<<grid, HEAT_BLOCK_THREADS, smem, s>>>(u, out, n, m, coef, ksteps);
 }
