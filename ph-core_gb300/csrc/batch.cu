@@ -386,6 +386,7 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
     const BTask& bt = b->host_tasks[i];
     for (int64_t j = 0; j < bt.nitems; j++) item_task[(size_t)(bt.item0 + j)] = (int32_t)i;
   }
+  for (phcu_program_t& P : b->host_progs) predecode_program(&P);
   cudaError_t e = cudaSuccess;
   const size_t nt = std::max<size_t>(1, b->host_tasks.size());
   if (e == cudaSuccess) e = cudaMalloc(&b->d_tasks, nt * sizeof(BTask));

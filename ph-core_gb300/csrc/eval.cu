@@ -102,6 +102,7 @@ static bool encode_tile_maps(const EvalPlan& p, TmaMaps* m) {
 int32_t launch_eval(const EvalArgs& A0) {
   if (A0.plan.nin < 0 || A0.plan.nin > MAXIN) return fail(PHCU_ERR_INVALID, "too many inputs (%d)", A0.plan.nin);
   EvalArgs A = A0;
+  predecode_program(&A.prog);
   TmaMaps maps;
   A.tma = encode_tile_maps(A.plan, &maps) ? &maps : nullptr;
   const bool narrow = program_is_32bit(A.prog, A.plan);

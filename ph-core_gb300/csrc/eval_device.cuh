@@ -33,9 +33,9 @@ __device__ __forceinline__ void row_group(const EvalPlan& p, const phcu_program_
   for (int u = 0; u < U; u++) {
     // a chunk past the end repeats chunk c0 (always valid): its values are
     // computed but not stored, so they raise no spurious status bits
-    uint32_t c = c0 + (uint32_t)u * cstep;
-    valid[u] = c < nchunks;
-    if (!valid[u]) c = c0;
+    const uint64_t c64 = (uint64_t)c0 + (uint64_t)u * cstep;
+    valid[u] = c64 < nchunks;
+    const uint32_t c = valid[u] ? (uint32_t)c64 : c0;
     uint32_t row, col;
     p.lendiv.divmod(c * VEC, row, col);
     off_out[u] = (int64_t)col * p.out.stride[W];

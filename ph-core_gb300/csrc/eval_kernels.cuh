@@ -41,6 +41,9 @@ __global__ void __launch_bounds__(ROW_THREADS, row_min_blocks<S, FAST>())
     eval_row_kernel(const __grid_constant__ EvalArgs A) {
   const uint32_t nchunks = (uint32_t)(A.plan.sp.n / VEC);
   const uint32_t nthreads = gridDim.x * blockDim.x;
+  // 64-bit position: the last steps may pass 2^32 when nchunks is close to it
+  const uint64_t first = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t step = (uint64_t)nthreads * U;
   uint32_t st = 0;
   if constexpr (FAST == FAST_NONE) {
     __shared__ __align__(16) phcu_program_t s_prog;
@@ -49,11 +52,11 @@ __global__ void __launch_bounds__(ROW_THREADS, row_min_blocks<S, FAST>())
     for (int i = threadIdx.x; i < WORDS; i += blockDim.x)
       reinterpret_cast<uint2*>(&s_prog)[i] = reinterpret_cast<const uint2*>(&A.prog)[i];
     __syncthreads();
-    for (uint32_t c0 = blockIdx.x * blockDim.x + threadIdx.x; c0 < nchunks; c0 += nthreads * U)
-      row_group<S, NIN, VEC, U, STASH, FAST>(A.plan, s_prog, c0, nthreads, nchunks, st);
+    for (uint64_t c0 = first; c0 < nchunks; c0 += step)
+      row_group<S, NIN, VEC, U, STASH, FAST>(A.plan, s_prog, (uint32_t)c0, nthreads, nchunks, st);
   } else {
-    for (uint32_t c0 = blockIdx.x * blockDim.x + threadIdx.x; c0 < nchunks; c0 += nthreads * U)
-      row_group<S, NIN, VEC, U, STASH, FAST>(A.plan, A.prog, c0, nthreads, nchunks, st);
+    for (uint64_t c0 = first; c0 < nchunks; c0 += step)
+      row_group<S, NIN, VEC, U, STASH, FAST>(A.plan, A.prog, (uint32_t)c0, nthreads, nchunks, st);
   }
   if (st) report_status(A.status, st);
 }

@@ -13,6 +13,7 @@
 // rounds once, as on the host.
 #pragma once
 
+#include <cstring>
 #include <type_traits>
 
 #include "common.cuh"
@@ -684,6 +685,122 @@ __device__ __forceinline__ void run_binop(const phcu_program_t& P, S* a, const S
   if (P.n_instr == 3) cvt_vec<S, V>(a, P.code[2].type, (int)P.code[2].imm.i);
 }
 
+// ------------------------------------------- pre-decoded arithmetic forms
+// The library's private copy of a program carries, in pad[0] of each
+// instruction, one of these ids when the instruction is a Float32 or Int32
+// operator whose operand B is an input or an immediate of the compute type.
+// The interpreter then runs it with one uniform branch on the operand source
+// and no operand copy, conversion check or type dispatch.  FX_NONE (0) leaves
+// the instruction to the general path.
+enum : uint8_t {
+  FX_NONE = 0,
+  FX_F32_LD, FX_F32_ADD, FX_F32_SUB, FX_F32_MUL, FX_F32_DIV, FX_F32_RSUB, FX_F32_RDIV,
+  FX_I32_LD, FX_I32_ADD, FX_I32_SUB, FX_I32_MUL, FX_I32_RSUB, FX_I32_WADD, FX_I32_WSUB, FX_I32_WMUL,
+  FX_I32_RWSUB, FX_I32_AND, FX_I32_OR, FX_I32_XOR,
+};
+
+// Host: writes the pre-decoded ids into a program copy (pad[0] of every
+// instruction; anything a caller left there is overwritten).  An Int32
+// immediate of a Float32 instruction is converted here, round to nearest as
+// the device conversion does, so the instruction qualifies.
+inline void predecode_program(phcu_program_t* P) {
+  for (int i = 0; i < P->n_instr && i < PHCU_MAX_INSTR; i++) {
+    phcu_instr_t& I = P->code[i];
+    I.pad[0] = FX_NONE;
+    if (!(I.src < MAXIN || I.src == PHCU_SRC_IMM)) continue;
+    if (I.src == PHCU_SRC_IMM && I.type == PHCU_F32 && I.btype == PHCU_I32 && I.op != PHCU_OP_POW) {
+      const float f = (float)(int32_t)(uint32_t)(uint64_t)I.imm.i;
+      uint32_t bits;
+      memcpy(&bits, &f, 4);
+      I.imm.i = (int64_t)bits;
+      I.btype = PHCU_F32;
+    }
+    if (I.btype != I.type) continue;
+    const bool swap = (I.flags & 1) != 0;
+    if (I.type == PHCU_F32) {
+      switch (I.op) {
+        case PHCU_I_LD: I.pad[0] = FX_F32_LD; break;
+        case PHCU_OP_ADD: I.pad[0] = FX_F32_ADD; break;
+        case PHCU_OP_MUL: I.pad[0] = FX_F32_MUL; break;
+        case PHCU_OP_SUB: I.pad[0] = swap ? FX_F32_RSUB : FX_F32_SUB; break;
+        case PHCU_OP_DIV: I.pad[0] = swap ? FX_F32_RDIV : FX_F32_DIV; break;
+      }
+    } else if (I.type == PHCU_I32) {
+      switch (I.op) {
+        case PHCU_I_LD: I.pad[0] = FX_I32_LD; break;
+        case PHCU_OP_ADD: I.pad[0] = FX_I32_ADD; break;
+        case PHCU_OP_MUL: I.pad[0] = FX_I32_MUL; break;
+        case PHCU_OP_SUB: I.pad[0] = swap ? FX_I32_RSUB : FX_I32_SUB; break;
+        case PHCU_OP_WADD: I.pad[0] = FX_I32_WADD; break;
+        case PHCU_OP_WMUL: I.pad[0] = FX_I32_WMUL; break;
+        case PHCU_OP_WSUB: I.pad[0] = swap ? FX_I32_RWSUB : FX_I32_WSUB; break;
+        case PHCU_OP_AND: I.pad[0] = FX_I32_AND; break;
+        case PHCU_OP_OR: I.pad[0] = FX_I32_OR; break;
+        case PHCU_OP_XOR: I.pad[0] = FX_I32_XOR; break;
+      }
+    }
+  }
+}
+
+// ACC = f(ACC, B) with B = the immediate or input `src`, chosen by one
+// uniform branch.
+template <typename S, int NIN, int V, typename F>
+__device__ __forceinline__ void fx_apply(int src, S imm, S* acc, const S (&in)[NIN > 0 ? NIN : 1][V], F f) {
+  if (src == PHCU_SRC_IMM) {
+    PHCU_LOOP acc[v] = f(acc[v], imm);
+    return;
+  }
+  if constexpr (NIN > 3) {
+    if (src == 3) {
+      PHCU_LOOP acc[v] = f(acc[v], in[3][v]);
+      return;
+    }
+  }
+  if constexpr (NIN > 2) {
+    if (src == 2) {
+      PHCU_LOOP acc[v] = f(acc[v], in[2][v]);
+      return;
+    }
+  }
+  if constexpr (NIN > 1) {
+    if (src == 1) {
+      PHCU_LOOP acc[v] = f(acc[v], in[1][v]);
+      return;
+    }
+  }
+  PHCU_LOOP acc[v] = f(acc[v], in[0][v]);
+}
+
+// Runs one pre-decoded instruction (fx != FX_NONE).
+template <typename S, int NIN, int V>
+__device__ __forceinline__ void run_fx(int fx, int src, S imm, S* acc, const S (&in)[NIN > 0 ? NIN : 1][V],
+                                       uint32_t& st) {
+#define PHCU_FX(ID, EXPR) \
+  case ID: fx_apply<S, NIN, V>(src, imm, acc, in, [&](S a, S b) -> S { return EXPR; }); break;
+  switch (fx) {
+    PHCU_FX(FX_F32_LD, b)
+    PHCU_FX(FX_F32_ADD, pf32<S>(sf32(a) + sf32(b)))
+    PHCU_FX(FX_F32_SUB, pf32<S>(sf32(a) - sf32(b)))
+    PHCU_FX(FX_F32_MUL, pf32<S>(sf32(a) * sf32(b)))
+    PHCU_FX(FX_F32_DIV, pf32<S>(sf32(a) / sf32(b)))
+    PHCU_FX(FX_F32_RSUB, pf32<S>(sf32(b) - sf32(a)))
+    PHCU_FX(FX_F32_RDIV, pf32<S>(sf32(b) / sf32(a)))
+    PHCU_FX(FX_I32_LD, b)
+    PHCU_FX(FX_I32_ADD, pi32<S>(chk_add32(si32(a), si32(b), st)))
+    PHCU_FX(FX_I32_SUB, pi32<S>(chk_sub32(si32(a), si32(b), st)))
+    PHCU_FX(FX_I32_MUL, pi32<S>(chk_mul32(si32(a), si32(b), st)))
+    PHCU_FX(FX_I32_RSUB, pi32<S>(chk_sub32(si32(b), si32(a), st)))
+    PHCU_FX(FX_I32_WADD, pi32<S>((int32_t)((uint32_t)a + (uint32_t)b)))
+    PHCU_FX(FX_I32_WSUB, pi32<S>((int32_t)((uint32_t)a - (uint32_t)b)))
+    PHCU_FX(FX_I32_WMUL, pi32<S>((int32_t)((uint32_t)a * (uint32_t)b)))
+    PHCU_FX(FX_I32_RWSUB, pi32<S>((int32_t)((uint32_t)b - (uint32_t)a)))
+    PHCU_FX(FX_I32_AND, pi32<S>((int32_t)((uint32_t)a & (uint32_t)b)))
+    PHCU_FX(FX_I32_OR, pi32<S>((int32_t)((uint32_t)a | (uint32_t)b)))
+    PHCU_FX(FX_I32_XOR, pi32<S>((int32_t)((uint32_t)a ^ (uint32_t)b)))
+  }
+#undef PHCU_FX
+}
+
 // ------------------------------------------------------ the interpreter
 // ACC = ACC op B on V elements in the compute type T (B already of type T, or
 // an integer exponent of a float power).
@@ -711,6 +828,11 @@ __device__ __forceinline__ void run_program(const phcu_program_t& P, const S (&i
   S s0[STASH ? V : 1], s1[STASH ? V : 1];
   const int ni = P.n_instr;
   for (int pc = 0; pc < ni; pc++) {
+    const int fx = P.code[pc].pad[0];
+    if (fx != FX_NONE) {
+      run_fx<S, NIN, V>(fx, P.code[pc].src, (S)(uint64_t)P.code[pc].imm.i, acc, in, st);
+      continue;
+    }
     const int op = P.code[pc].op;
     const int T = P.code[pc].type;
     if constexpr (STASH) {
