@@ -653,6 +653,22 @@ class _Indexable:
     def __repr__(self):
         return "%s(%s, %s)" % (type(self).__name__, "x".join(map(str, self._shape)), A.DTYPE_NAMES[self.dtype])
 
+    # ---------------------------------------------------------- printing
+    def to_s(self, settings=None):
+        """MultiIndexable#to_s (formatter/formatter.cr:304-315): only the
+        displayed elements are gathered on the device and downloaded."""
+        from . import formatter
+
+        return formatter.to_s(self, settings)
+
+    __str__ = to_s
+
+    def to_literal_s(self):
+        """MultiIndexable#to_literal_s (formatter/formatter.cr:298-300)."""
+        from . import formatter
+
+        return formatter.to_literal_s(self)
+
 
 _OP_NAMES = {A.OP_ADD: "+", A.OP_SUB: "-", A.OP_MUL: "*", A.OP_DIV: "/", A.OP_FLOORDIV: "//", A.OP_MOD: "%",
              A.OP_POW: "**", A.OP_WADD: "&+", A.OP_WSUB: "&-", A.OP_WMUL: "&*", A.OP_WPOW: "&**",

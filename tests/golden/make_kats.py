@@ -155,6 +155,36 @@ def kats():
         "compatible": [[2, 5, 3, 1, 1], [1, 2, 1, 1], [4, 6, 3, 2, 1, 1, 1, 1, 1], [1], []],
         "incompatible": [[2, 5], [2, 1, 1], [4, 3, 2, 1, 1, 1, 1, 1], [-2], [1]],
     }
+    # Formatter output (colours off).  README.md:29-37: `puts narr`, `puts narr2`
+    # (header line and body); src/multi_indexable/formatter/settings.cr:53-79:
+    # the body printed for NArray.build([2, 2, 2, 2]) { |_, idx| idx } with
+    # brackets [{"<", ">"}, {"begin", "end"}] (the doc comment shows no header).
+    k["formatter"] = {
+        "readme_narr": {"elements": [[1, 0, 0], [0, 1, 0]],
+                        "text": "2x3 Phase::NArray(Int32)\n[[1, 0, 0],\n [0, 1, 0]]"},
+        "readme_narr2": {"elements": [[0, 1, 2], [10, 11, 12]],
+                         "text": "2x3 Phase::NArray(Int32)\n[[ 0,  1,  2],\n [10, 11, 12]]"},
+        "brackets_4d": {
+            "shape": [2, 2, 2, 2], "brackets": [["<", ">"], ["begin", "end"]],
+            "body": "\n".join([
+                "begin",
+                "    <",
+                "        begin< 0,  1>,",
+                "             < 2,  3>end,",
+                "        ",
+                "        begin< 4,  5>,",
+                "             < 6,  7>end",
+                "    >,",
+                "    <",
+                "        begin< 8,  9>,",
+                "             <10, 11>end,",
+                "        ",
+                "        begin<12, 13>,",
+                "             <14, 15>end",
+                "    >",
+                "end"]),
+        },
+    }
     return k
 
 
