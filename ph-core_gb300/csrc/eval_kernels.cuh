@@ -26,10 +26,12 @@ constexpr int min_blocks() {
 }
 
 // ROW kernels of 32-bit in-place binary operators hold little besides their
-// operands: four resident blocks (64 registers) keep more loads in flight.
+// operands: six resident blocks of 8 elements per thread (40 registers) beat
+// four of 16 (reversed-view binaries 145 -> 139 us, Float32 division
+// 155 -> 127 us on 512x512x256); eight blocks were slower (158 us).
 template <typename S, int FAST>
 constexpr int row_min_blocks() {
-  return (FAST == FAST_BINOP && sizeof(S) == 4) ? 4 : min_blocks<FAST>();
+  return (FAST == FAST_BINOP && sizeof(S) == 4) ? 6 : min_blocks<FAST>();
 }
 
 // ROW: each thread handles U grid-strided chunks of VEC elements per iteration.
@@ -88,12 +90,15 @@ static int32_t launch_grid(K kernel, const EvalArgs& A, uint64_t work_blocks, in
 }
 
 // Elements per thread per iteration: enough independent loads in flight
-// without pushing the register count past the residency target (copies and
-// in-place binary operators carry no interpreter state; stash registers cost
-// the most).
+// without pushing the register count past the residency target (copies carry
+// no interpreter state; stash registers cost the most).  32-bit binary
+// operators take 8 and more resident blocks instead (row_min_blocks); more
+// elements per thread were slower for every kernel measured (16 for
+// interpreted programs: 233 -> 338 us on the fused chain).
 template <typename S, bool STASH, int FAST>
 constexpr int elements_per_thread() {
-  return FAST != FAST_NONE ? (sizeof(S) == 4 ? 16 : 8) : STASH ? 4 : (sizeof(S) == 4 ? 8 : 4);
+  return FAST != FAST_NONE ? (sizeof(S) == 4 ? (FAST == FAST_BINOP ? 8 : 16) : 8)
+                           : STASH ? 4 : (sizeof(S) == 4 ? 8 : 4);
 }
 
 template <typename S, int NIN, int VEC, bool STASH, int FAST>

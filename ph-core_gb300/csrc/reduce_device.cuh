@@ -51,6 +51,8 @@ struct Lim;
 template <>
 struct Lim<float> {
   static __device__ __forceinline__ bool nan(float x) { return x != x; }
+  // the extreme of a and b ignoring a NaN operand (fmaxf/fminf return the other one)
+  static __device__ __forceinline__ float ext(float a, float b, bool is_max) { return is_max ? fmaxf(a, b) : fminf(a, b); }
 };
 template <>
 struct Lim<double> {
@@ -59,6 +61,7 @@ struct Lim<double> {
 template <>
 struct Lim<int32_t> {
   static __device__ __forceinline__ bool nan(int32_t) { return false; }
+  static __device__ __forceinline__ int32_t ext(int32_t a, int32_t b, bool is_max) { return is_max ? max(a, b) : min(a, b); }
 };
 template <>
 struct Lim<long long> {
@@ -420,6 +423,32 @@ __device__ __forceinline__ void vec_extreme_into(ExtAcc<T>& acc, const T* x, int
   if (be >= 0) acc.add(bv, k0 + be, is_max);
 }
 
+// Folds U vectors of VN elements of 4-byte type (element (u, e) at index
+// k + u * stride + e, so increasing (u, e) is increasing index) into an
+// extremum accumulator: the extreme value m over the non-NaN elements (one
+// min/max per element), then the first element equal to m (a compare and a
+// select per element), offered to the accumulator once.  That element is the
+// one a strict-comparison scan skipping NaNs keeps.  Its value is m itself,
+// except for zeros, whose sign is taken from the element found.
+template <typename T, int U, int VN>
+__device__ __forceinline__ void block_extreme_into(ExtAcc<T>& acc, const T (&x)[U][VN], int64_t k, int64_t stride,
+                                                   bool is_max) {
+  T m = x[0][0];
+#pragma unroll
+  for (int t = 1; t < U * VN; t++) m = Lim<T>::ext(m, x[t / VN][t % VN], is_max);
+  int j = -1;
+#pragma unroll
+  for (int t = U * VN - 1; t >= 0; t--) j = (x[t / VN][t % VN] == m) ? t : j;
+  if (j < 0) return;  // every element NaN
+  T val = m;
+  if (m == (T)0) {
+#pragma unroll
+    for (int t = 0; t < U * VN; t++)
+      if (t == j) val = x[t / VN][t % VN];
+  }
+  acc.add(val, k + (int64_t)(j / VN) * stride + (j % VN), is_max);
+}
+
 // GROUP with 16-byte loads along a contiguous reduced axis: lane l of a group
 // of G reads vectors l, l + G, l + 2G, ... of each of NO outputs (elements of
 // one accumulator arrive in increasing k), then the < VN elements past the last
@@ -452,16 +481,21 @@ __device__ __forceinline__ void group_vec(const RedArgs& a, int64_t o0, int64_t 
 #pragma unroll
       for (int u = 0; u < U; u++) ld16<T>(base[q] + (k + (int64_t)u * G * VN) * (int64_t)sizeof(T), x[q][u]);
 #pragma unroll
-    for (int q = 0; q < NO; q++)
+    for (int q = 0; q < NO; q++) {
+      if constexpr (KIND != RK_SUM && sizeof(T) == 4) {
+        block_extreme_into<T, U, VN>(eacc[q], x[q], k, (int64_t)G * VN, is_max);
+      } else {
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        if (KIND == RK_SUM) {
+        for (int u = 0; u < U; u++) {
+          if (KIND == RK_SUM) {
 #pragma unroll
-          for (int e = 0; e < VN; e++) sacc[q].add(x[q][u][e]);
-        } else {
-          vec_extreme_into<T, VN>(eacc[q], x[q][u], k + (int64_t)u * G * VN, is_max);
+            for (int e = 0; e < VN; e++) sacc[q].add(x[q][u][e]);
+          } else {
+            vec_extreme_into<T, VN>(eacc[q], x[q][u], k + (int64_t)u * G * VN, is_max);
+          }
         }
       }
+    }
   }
   for (; k + VN <= kv1; k += (int64_t)G * VN) {
 #pragma unroll
