@@ -189,6 +189,20 @@ PHCU_API int32_t phcu_host_free(void* hptr);
 PHCU_API int32_t phcu_upload(void* dst, const void* src, size_t bytes);
 /* Device -> host copy; returns when the data is on the host (to_narr). */
 PHCU_API int32_t phcu_download(void* dst, const void* src, size_t bytes);
+/* Overlapped transfers (the bulk copies behind NArray#to_narr / of_buffer,
+ * src/view.cr:123-126, src/n_array.cr:76-79, for callers that pipeline many
+ * results).  phcu_download_async starts a device -> host copy that waits for
+ * the work enqueued so far and then runs on the library's device-to-host
+ * stream while later kernels proceed; phcu_upload_async copies host -> device
+ * on a host-to-device stream after the work enqueued so far, and later
+ * library work waits for it (it does not wait for outstanding downloads).
+ * Until phcu_transfer_wait (or phcu_sync) returns, the host buffers must stay
+ * untouched and pinned (phcu_host_alloc), a download's source must not be
+ * written or freed, and an upload's destination must not be the source of an
+ * unfinished download. */
+PHCU_API int32_t phcu_download_async(void* dst, const void* src, size_t bytes);
+PHCU_API int32_t phcu_upload_async(void* dst, const void* src, size_t bytes);
+PHCU_API int32_t phcu_transfer_wait(void);
 PHCU_API int32_t phcu_memset(void* dptr, int32_t value, size_t bytes);
 
 /* ---------------------------------------------------------------- hot path */

@@ -45,6 +45,10 @@ struct Context {
   void* l2_scrub = nullptr;
   size_t l2_scrub_bytes = 0;
   unsigned long long launches = 0;
+  // transfers that run behind the library stream's kernels (one stream per
+  // copy direction, so both copy engines and the SMs work at once)
+  cudaStream_t d2h = nullptr, h2d = nullptr;
+  cudaEvent_t ev_work = nullptr, ev_h2d = nullptr;
 };
 Context& ctx();
 int32_t require_ctx();

@@ -87,6 +87,10 @@ int32_t phcu_init(int32_t device) {
     uint64_t thr = UINT64_MAX;
     cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
   }
+  PHCU_CUDA(cudaStreamCreateWithFlags(&c.d2h, cudaStreamNonBlocking));
+  PHCU_CUDA(cudaStreamCreateWithFlags(&c.h2d, cudaStreamNonBlocking));
+  PHCU_CUDA(cudaEventCreateWithFlags(&c.ev_work, cudaEventDisableTiming));
+  PHCU_CUDA(cudaEventCreateWithFlags(&c.ev_h2d, cudaEventDisableTiming));
   c.device = device;
   c.launches = 0;
   c.ready = true;
@@ -97,8 +101,14 @@ int32_t phcu_shutdown(void) {
   Context& c = g_ctx;
   if (!c.ready) return PHCU_OK;
   cudaStreamSynchronize(c.stream);
+  cudaStreamSynchronize(c.d2h);
+  cudaStreamSynchronize(c.h2d);
   if (c.l2_scrub) cudaFree(c.l2_scrub);
   cudaFree(c.status);
+  cudaEventDestroy(c.ev_work);
+  cudaEventDestroy(c.ev_h2d);
+  cudaStreamDestroy(c.d2h);
+  cudaStreamDestroy(c.h2d);
   cudaStreamDestroy(c.own_stream);
   c = Context();
   return PHCU_OK;
@@ -119,6 +129,8 @@ int32_t phcu_get_stream(void** s) {
 int32_t phcu_sync(void) {
   PHCU_TRY(require_ctx());
   PHCU_CUDA(cudaStreamSynchronize(g_ctx.stream));
+  PHCU_CUDA(cudaStreamSynchronize(g_ctx.d2h));
+  PHCU_CUDA(cudaStreamSynchronize(g_ctx.h2d));
   return PHCU_OK;
 }
 
@@ -196,6 +208,41 @@ int32_t phcu_download(void* dst, const void* src, size_t bytes) {
   if (bytes == 0) return PHCU_OK;
   PHCU_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g_ctx.stream));
   PHCU_CUDA(cudaStreamSynchronize(g_ctx.stream));
+  return PHCU_OK;
+}
+
+// Device -> host behind the library stream: the copy waits for the work
+// enqueued so far (an event on the library stream), then runs on the
+// device-to-host stream while later kernels proceed.
+int32_t phcu_download_async(void* dst, const void* src, size_t bytes) {
+  PHCU_TRY(require_ctx());
+  if (bytes == 0) return PHCU_OK;
+  if (!dst || !src) return fail(PHCU_ERR_INVALID, "phcu_download_async: null pointer");
+  PHCU_CUDA(cudaEventRecord(g_ctx.ev_work, g_ctx.stream));
+  PHCU_CUDA(cudaStreamWaitEvent(g_ctx.d2h, g_ctx.ev_work, 0));
+  PHCU_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g_ctx.d2h));
+  return PHCU_OK;
+}
+
+// Host -> device on the host-to-device stream: it waits for the work enqueued
+// so far (which may still read dst), and later library work waits for it.
+// Outstanding downloads are not waited for, so an upload overlaps them.
+int32_t phcu_upload_async(void* dst, const void* src, size_t bytes) {
+  PHCU_TRY(require_ctx());
+  if (bytes == 0) return PHCU_OK;
+  if (!dst || !src) return fail(PHCU_ERR_INVALID, "phcu_upload_async: null pointer");
+  PHCU_CUDA(cudaEventRecord(g_ctx.ev_work, g_ctx.stream));
+  PHCU_CUDA(cudaStreamWaitEvent(g_ctx.h2d, g_ctx.ev_work, 0));
+  PHCU_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g_ctx.h2d));
+  PHCU_CUDA(cudaEventRecord(g_ctx.ev_h2d, g_ctx.h2d));
+  PHCU_CUDA(cudaStreamWaitEvent(g_ctx.stream, g_ctx.ev_h2d, 0));
+  return PHCU_OK;
+}
+
+int32_t phcu_transfer_wait(void) {
+  PHCU_TRY(require_ctx());
+  PHCU_CUDA(cudaStreamSynchronize(g_ctx.d2h));
+  PHCU_CUDA(cudaStreamSynchronize(g_ctx.h2d));
   return PHCU_OK;
 }
 

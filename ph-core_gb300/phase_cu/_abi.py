@@ -123,6 +123,9 @@ _SIGS = [
     ("phcu_host_free", [_vp]),
     ("phcu_upload", [_vp, _vp, ctypes.c_size_t]),
     ("phcu_download", [_vp, _vp, ctypes.c_size_t]),
+    ("phcu_download_async", [_vp, _vp, ctypes.c_size_t]),
+    ("phcu_upload_async", [_vp, _vp, ctypes.c_size_t]),
+    ("phcu_transfer_wait", []),
     ("phcu_memset", [_vp, ctypes.c_int32, ctypes.c_size_t]),
     ("phcu_copy", [_P(View), _P(View)]),
     ("phcu_fill", [_P(View), _P(Scalar)]),
