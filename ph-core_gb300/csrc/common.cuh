@@ -56,6 +56,13 @@ inline cudaStream_t stream() { return ctx().stream; }
 inline void count_launch(unsigned n = 1) { ctx().launches += n; }
 int32_t check_launch(const char* what);
 
+// Resident blocks per SM of kernel `fn` at this block size and dynamic
+// shared memory, asked of the runtime once per (kernel, threads, smem) and
+// remembered: the query costs host time that would otherwise come with every
+// launch.  Raises the kernel's dynamic shared-memory limit first when smem
+// exceeds the 48 KB default (only ever upwards, once per new maximum).
+int blocks_per_sm(const void* fn, int threads, size_t smem);
+
 // stream-ordered scratch
 int32_t scratch_alloc(size_t bytes, void** p);
 void scratch_free(void* p);

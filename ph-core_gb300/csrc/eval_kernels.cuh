@@ -77,10 +77,7 @@ template <typename K>
 static int32_t launch_grid(K kernel, const EvalArgs& A, uint64_t work_blocks, int threads, size_t smem,
                            const char* what) {
   Context& c = ctx();
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-  if (per_sm < 1) per_sm = 1;
+  const int per_sm = blocks_per_sm((const void*)kernel, threads, smem);
   uint64_t grid = (uint64_t)c.sm_count * per_sm;
   if (grid > work_blocks) grid = work_blocks;
   if (grid < 1) grid = 1;

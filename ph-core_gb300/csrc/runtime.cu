@@ -58,6 +58,41 @@ struct Timer {
   cudaEvent_t a, b;
 };
 
+// Launch-shape cache of blocks_per_sm (one host thread per context).
+struct OccEntry {
+  const void* fn;
+  int threads;
+  size_t smem;
+  int per_sm;
+};
+struct SmemLimit {
+  const void* fn;
+  size_t smem;
+};
+static OccEntry g_occ[256];
+static int g_nocc = 0;
+static SmemLimit g_lim[128];
+static int g_nlim = 0;
+
+int blocks_per_sm(const void* fn, int threads, size_t smem) {
+  if (smem > 48 * 1024) {
+    int i = 0;
+    while (i < g_nlim && g_lim[i].fn != fn) i++;
+    if (i == g_nlim || g_lim[i].smem < smem) {
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (i < g_nlim) g_lim[i].smem = smem;
+      else if (g_nlim < 128) g_lim[g_nlim++] = {fn, smem};
+    }
+  }
+  for (int i = 0; i < g_nocc; i++)
+    if (g_occ[i].fn == fn && g_occ[i].threads == threads && g_occ[i].smem == smem) return g_occ[i].per_sm;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+  if (per_sm < 1) per_sm = 1;
+  if (g_nocc < 256) g_occ[g_nocc++] = {fn, threads, smem, per_sm};
+  return per_sm;
+}
+
 }  // namespace phcu
 
 using namespace phcu;
@@ -111,6 +146,8 @@ int32_t phcu_shutdown(void) {
   cudaStreamDestroy(c.h2d);
   cudaStreamDestroy(c.own_stream);
   c = Context();
+  g_nocc = 0;  // attributes and occupancy belong to this device's context
+  g_nlim = 0;
   return PHCU_OK;
 }
 

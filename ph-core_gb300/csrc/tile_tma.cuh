@@ -345,10 +345,7 @@ static int32_t launch_tma(const EvalArgs& A) {
   auto kernel = eval_tma_kernel<S, NIN, STASH, FAST>;
   const size_t smem = tma_smem_bytes(A.plan.staged);
   Context& c = ctx();
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, TILE_THREADS, smem);
-  if (per_sm < 1) per_sm = 1;
+  const int per_sm = blocks_per_sm((const void*)kernel, TILE_THREADS, smem);
   const uint64_t ntiles = (uint64_t)A.plan.tiles_w * A.plan.tiles_r * A.plan.nbatch;
   uint64_t grid = (uint64_t)c.sm_count * per_sm;
   if (grid > ntiles) grid = ntiles;
