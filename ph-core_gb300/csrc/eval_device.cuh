@@ -16,8 +16,10 @@ namespace phcu {
 constexpr int TILE_THREADS = 256;
 
 // FAST selects how the per-element work runs: the interpreter (FAST_NONE), a
-// plain move (FAST_COPY) or an in-place binary operator (FAST_BINOP).
-enum : int { FAST_NONE = 0, FAST_COPY = 1, FAST_BINOP = 2 };
+// plain move (FAST_COPY), an in-place binary operator (FAST_BINOP) or the
+// interpreter reduced to pre-decoded instructions (FAST_FX, program_is_fx).
+enum : int { FAST_NONE = 0, FAST_COPY = 1, FAST_BINOP = 2, FAST_FX = 3 };
+constexpr bool interpreted(int fast) { return fast == FAST_NONE || fast == FAST_FX; }
 
 // ----------------------------------------------------------------- ROW
 // U chunks of VEC consecutive elements: chunk u is c0 + u * cstep.
@@ -84,6 +86,8 @@ __device__ __forceinline__ void row_group(const EvalPlan& p, const phcu_program_
     run_binop<S, V>(prog, in[0], in[1], st);
 #pragma unroll
     for (int v = 0; v < V; v++) acc[v] = in[0][v];
+  } else if constexpr (FAST == FAST_FX) {
+    run_program_fx<S, NIN, V>(prog, in, acc, st);
   } else {
     run_program<S, NIN, V, STASH>(prog, in, acc, st);
   }
@@ -228,7 +232,7 @@ __device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_
   constexpr int NWARP = TILE_THREADS / 32;
   // rows per pass: 8 (16 elements per thread) for copies and in-place binary
   // operators, 4 (8 elements) for interpreted programs; half with 64-bit slots
-  constexpr int NI = (FAST != FAST_NONE ? 8 : 4) / (sizeof(S) == 4 ? 1 : 2);
+  constexpr int NI = (!interpreted(FAST) ? 8 : 4) / (sizeof(S) == 4 ? 1 : 2);
   constexpr int V = NI * (TILE / 32);
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -336,6 +340,8 @@ __device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_
       run_binop<S, V>(prog, in[0], in[1], st);
 #pragma unroll
       for (int v = 0; v < V; v++) acc[v] = in[0][v];
+    } else if constexpr (FAST == FAST_FX) {
+      run_program_fx<S, NIN, V>(prog, in, acc, st);
     } else {
       run_program<S, NIN, V, STASH>(prog, in, acc, st);
     }

@@ -25,13 +25,15 @@ constexpr int min_blocks() {
   return FAST == FAST_COPY ? 4 : 3;
 }
 
-// ROW kernels of 32-bit in-place binary operators hold little besides their
-// operands: six resident blocks of 8 elements per thread (40 registers) beat
-// four of 16 (reversed-view binaries 145 -> 139 us, Float32 division
-// 155 -> 127 us on 512x512x256); eight blocks were slower (158 us).
+// ROW kernels of 32-bit in-place binary operators: 8 elements per thread at
+// four resident blocks per SM.  Reversed-view binaries on 512x512x256 took
+// 123 us per launch so (three blocks: 123, five: 129, six: 138, eight: 158;
+// 16 elements at four blocks: 145; 32 at two: 200).  The ROW kernel of a
+// pre-decoded 32-bit program fits 64 registers without spills: four resident
+// blocks instead of three (fused chain 220 -> 187 us).
 template <typename S, int FAST>
 constexpr int row_min_blocks() {
-  return (FAST == FAST_BINOP && sizeof(S) == 4) ? 6 : min_blocks<FAST>();
+  return (FAST == FAST_BINOP && sizeof(S) == 4) ? 4 : (FAST == FAST_FX && sizeof(S) == 4) ? 4 : min_blocks<FAST>();
 }
 
 // ROW: each thread handles U grid-strided chunks of VEC elements per iteration.
@@ -47,7 +49,7 @@ __global__ void __launch_bounds__(ROW_THREADS, row_min_blocks<S, FAST>())
   const uint64_t first = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint64_t step = (uint64_t)nthreads * U;
   uint32_t st = 0;
-  if constexpr (FAST == FAST_NONE) {
+  if constexpr (interpreted(FAST)) {
     __shared__ __align__(16) phcu_program_t s_prog;
     static_assert(sizeof(phcu_program_t) % 8 == 0, "program copied in 8-byte words");
     constexpr int WORDS = (int)(sizeof(phcu_program_t) / 8);
@@ -94,8 +96,8 @@ static int32_t launch_grid(K kernel, const EvalArgs& A, uint64_t work_blocks, in
 // interpreted programs: 233 -> 338 us on the fused chain).
 template <typename S, bool STASH, int FAST>
 constexpr int elements_per_thread() {
-  return FAST != FAST_NONE ? (sizeof(S) == 4 ? (FAST == FAST_BINOP ? 8 : 16) : 8)
-                           : STASH ? 4 : (sizeof(S) == 4 ? 8 : 4);
+  return !interpreted(FAST) ? (sizeof(S) == 4 ? (FAST == FAST_BINOP ? 8 : 16) : 8)
+                            : STASH ? 4 : (sizeof(S) == 4 ? 8 : 4);
 }
 
 template <typename S, int NIN, int VEC, bool STASH, int FAST>
@@ -153,6 +155,8 @@ int32_t launch_eval_sn(const EvalArgs& A) {
     if (program_is_binop(A.prog, A.plan))
       return tile ? launch_tile_any<S, NIN, false, FAST_BINOP>(A) : launch_row<S, NIN, false, FAST_BINOP>(A);
   }
+  if (!stash && program_is_fx(A.prog))
+    return tile ? launch_tile_any<S, NIN, false, FAST_FX>(A) : launch_row<S, NIN, false, FAST_FX>(A);
   if (tile) return stash ? launch_tile_any<S, NIN, true, FAST_NONE>(A) : launch_tile_any<S, NIN, false, FAST_NONE>(A);
   return stash ? launch_row<S, NIN, true, FAST_NONE>(A) : launch_row<S, NIN, false, FAST_NONE>(A);
 }

@@ -801,6 +801,40 @@ __device__ __forceinline__ void run_fx(int fx, int src, S imm, S* acc, const S (
 #undef PHCU_FX
 }
 
+// A program every instruction of which has a pre-decoded form or is
+// `Float ** Int` with an immediate exponent (host check: program_is_fx).
+// Kernels built for such programs compile only these two paths: no operand
+// copies, conversions or type dispatch, so they need fewer registers.
+inline bool program_is_fx(const phcu_program_t& P) {
+  if (P.n_instr < 1) return false;
+  for (int i = 0; i < P.n_instr; i++) {
+    const phcu_instr_t& I = P.code[i];
+    if (I.pad[0] != FX_NONE) continue;
+    if (I.op == PHCU_OP_POW && I.src == PHCU_SRC_IMM && is_float_t(I.type) && is_int_t(I.btype) && !(I.flags & 1))
+      continue;
+    return false;
+  }
+  return true;
+}
+
+template <typename S, int V>
+__device__ __forceinline__ void powi_uniform(S* a, int T, int32_t e);
+
+template <typename S, int NIN, int V>
+__device__ __forceinline__ void run_program_fx(const phcu_program_t& P, const S (&in)[NIN > 0 ? NIN : 1][V],
+                                               S (&acc)[V], uint32_t& st) {
+  const int ni = P.n_instr;
+  for (int pc = 0; pc < ni; pc++) {
+    const int fx = P.code[pc].pad[0];
+    if (fx != FX_NONE) {
+      run_fx<S, NIN, V>(fx, P.code[pc].src, (S)(uint64_t)P.code[pc].imm.i, acc, in, st);
+    } else {
+      const int64_t e = P.code[pc].imm.i;
+      powi_uniform<S, V>(acc, P.code[pc].type, P.code[pc].btype == PHCU_I32 ? (int32_t)(uint32_t)e : (int32_t)e);
+    }
+  }
+}
+
 // ------------------------------------------------------ the interpreter
 // ACC = ACC op B on V elements in the compute type T (B already of type T, or
 // an integer exponent of a float power).

@@ -225,6 +225,8 @@ __device__ __forceinline__ void tma_tile_body(const EvalPlan& p, const phcu_prog
       run_binop<S, V>(prog, in[0], in[1], st);
 #pragma unroll
       for (int v = 0; v < V; v++) acc[v] = in[0][v];
+    } else if constexpr (FAST == FAST_FX) {
+      run_program_fx<S, NIN, V>(prog, in, acc, st);
     } else {
       run_program<S, NIN, V, STASH>(prog, in, acc, st);
     }
