@@ -274,26 +274,19 @@ def displayed_ranges(shape, settings):
     return out
 
 
-def gather_displayed(arr, settings):
-    """The displayed elements of a device array as a compact host array: one
-    strided device copy per corner block of the displayed index product, then
-    one download."""
+def _compact_on_device(arr, ranges):
+    """A new device array holding the elements of the device view `arr` at the
+    product of the per-axis index ranges: one strided copy per corner block."""
     from .narray import CuNArray, _copy_into, _make_view, _row_major
 
-    shape = list(arr.shape)
-    ranges = displayed_ranges(shape, settings)
     kshape = [sum(b - a for a, b in r) for r in ranges]
-    if any(n == 0 for n in kshape):
-        return np.empty(kshape, dtype=arr.np_dtype)
-    if kshape == shape and isinstance(arr, CuNArray):
-        return arr.to_narr()
     out = CuNArray.empty(kshape, arr.dtype)
+    if any(n == 0 for n in kshape):
+        return out
     buf, off, _, stride = arr._desc()
     ostride = _row_major(kshape)
-    rank = len(shape)
-    # every combination of one range per axis
     combos = [[]]
-    for d in range(rank):
+    for d in range(len(ranges)):
         combos = [c + [(d, i)] for c in combos for i in range(len(ranges[d]))]
     for combo in combos:
         soff, doff, bshape = off, 0, []
@@ -303,10 +296,30 @@ def gather_displayed(arr, settings):
             soff += a * stride[d]
             doff += pos * ostride[d]
             bshape.append(b - a)
-        src = _make_view(buf, arr.dtype, soff, bshape, stride)
-        dst = _make_view(out._buf, arr.dtype, doff, bshape, ostride)
-        _copy_into(dst, src)
-    return out.to_narr()
+        _copy_into(_make_view(out._buf, arr.dtype, doff, bshape, ostride), _make_view(buf, arr.dtype, soff, bshape, stride))
+    return out
+
+
+def gather_displayed(arr, settings):
+    """The displayed elements of a device array as a compact host array: one
+    strided device copy per corner block of the displayed index product, then
+    one download.  A lazy CuProcView gathers the displayed elements of each of
+    its operand views and runs its fused program on those alone, as the
+    reference's ProcView computes only the elements it is asked for."""
+    from .narray import CuNArray, CuProcView
+
+    shape = list(arr.shape)
+    ranges = displayed_ranges(shape, settings)
+    kshape = [sum(b - a for a, b in r) for r in ranges]
+    if any(n == 0 for n in kshape):
+        return np.empty(kshape, dtype=arr.np_dtype)
+    if isinstance(arr, CuProcView):
+        leaves = [CuProcView._leaf(_compact_on_device(v, ranges)) for v in arr._leaves]
+        compact = CuProcView([x._leaves[0] for x in leaves], arr._expr, arr.dtype, kshape)
+        return compact.to_narr()
+    if kshape == shape and isinstance(arr, CuNArray):
+        return arr.to_narr()
+    return _compact_on_device(arr, ranges).to_narr()
 
 
 # ---------------------------------------------------------- element text

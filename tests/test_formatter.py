@@ -181,3 +181,19 @@ def test_device_views_print_like_their_host_copy(cu):
     assert str(v).split("\n", 1)[1] == FO.format_body(host, _oracle_settings(s))
     assert v.to_literal_s() == FO.format_literal(host)
     assert str(X[cu.R(1, -1, 2), 3]).split("\n", 1)[1] == FO.format_body(a[1::2, 3], _oracle_settings(s))
+
+
+@pytest.mark.gpu
+def test_device_proc_view_prints_its_displayed_elements(cu):
+    """A lazy ProcView gathers the displayed elements of its operands and runs
+    its fused program on those alone; the text equals the full result's."""
+    rng = np.random.default_rng(9)
+    a = (rng.standard_normal((40, 33, 21)) * 10).astype(np.float32)
+    b = (rng.standard_normal((40, 33, 21)) * 10).astype(np.float32)
+    X, Y = cu.CuNArray.from_numpy(a), cu.CuNArray.from_numpy(b)
+    pv = X.view().process(lambda e: (e + 4) ** 2) * Y.view().reverse() - X.view()
+    full = pv.to_narr()
+    s = F.Settings.default()
+    assert str(pv).split("\n", 1)[1] == FO.format_body(full, _oracle_settings(s))
+    small = X.view(slice(0, 3), 0, slice(0, 4)).process(lambda e: e * 2)
+    assert str(small).split("\n", 1)[1] == FO.format_body(small.to_narr(), _oracle_settings(s))
