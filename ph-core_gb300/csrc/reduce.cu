@@ -112,7 +112,10 @@ static int32_t launch_typed(const RedArgs& a, const RedShape& sh) {
   constexpr int VN = 16 / sizeof(T);
   // four outputs per group when the reduced axis is short and outputs are many
   const bool four = sh.mode == 0 && a.K <= (sh.vec ? 2 * VN : 8) * sh.G && a.O >= 4096;
-  int64_t work_threads = (sh.mode == 0) ? (four ? (a.O + 3) / 4 : a.O) * a.S * sh.G
+  // two outputs per group for an extremum whose rows one pass of the group covers: eight vectors in
+  // flight per lane (axis-3 max/argmax of 64x128x128x64 68 -> 63 us; sums lose, 57 -> 65 us)
+  const bool two = !four && KIND == RK_EXT && sh.mode == 0 && sh.vec && a.K <= 4 * VN * sh.G && a.O >= 4096;
+  int64_t work_threads = (sh.mode == 0) ? (four ? (a.O + 3) / 4 : two ? (a.O + 1) / 2 : a.O) * a.S * sh.G
                                         : (sh.vec ? a.O / VN : a.O) * a.S;
   int64_t blocks = (work_threads + threads - 1) / threads;
   int64_t cap = (int64_t)c.sm_count * 8 * 4;
@@ -126,6 +129,13 @@ static int32_t launch_typed(const RedArgs& a, const RedShape& sh) {
       case 16: reduce_group_vec_kernel<T, KIND, 16, 4><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
       case 8: reduce_group_vec_kernel<T, KIND, 8, 4><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
       default: reduce_group_vec_kernel<T, KIND, 4, 4><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+    }
+  } else if (sh.vec && two) {
+    switch (sh.G) {
+      case 32: reduce_group_vec_kernel<T, KIND, 32, 2><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      case 16: reduce_group_vec_kernel<T, KIND, 16, 2><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      case 8: reduce_group_vec_kernel<T, KIND, 8, 2><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
+      default: reduce_group_vec_kernel<T, KIND, 4, 2><<<(unsigned)blocks, threads, 0, c.stream>>>(a); break;
     }
   } else if (sh.vec) {
     switch (sh.G) {

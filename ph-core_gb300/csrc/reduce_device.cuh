@@ -458,7 +458,7 @@ template <typename T, int KIND, int G, int NO>
 __device__ __forceinline__ void group_vec(const RedArgs& a, int64_t o0, int64_t split, int glane, unsigned gmask,
                                           uint32_t& st) {
   constexpr int VN = 16 / sizeof(T);
-  constexpr int U = NO == 1 ? 4 : 1;  // vectors in flight per output and lane
+  constexpr int U = NO <= 2 ? 4 : 1;  // vectors in flight per output and lane
   const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
   const int64_t k0 = split * a.chunk;
   const int64_t k1 = min(a.K, k0 + a.chunk);
