@@ -8,8 +8,11 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
+# [4099, 48] and [4097, 61] along axis 1: an odd number of outputs whose rows
+# one pass of a group covers (the extremum takes two outputs per group), the
+# second with a partial last vector
 SHAPES = [[64, 8, 8, 64], [3, 1000], [1000, 3], [7, 4097], [2, 3, 5, 8], [1, 300001], [300000, 1], [16, 4096],
-          [4096, 16], [5, 6, 7]]
+          [4096, 16], [5, 6, 7], [4099, 48], [4097, 61]]
 
 
 def _arr(x):
