@@ -161,8 +161,9 @@ def make_jobs(cu, A, dev, n):
                 for op in ops:
                     out = o64 if (op == A.OP_DIV and dt == "i32") else o
                     nbytes = 2 * n * es + n * (8 if out is o64 else es)
-                    jobs.append(("binary_" + kind, "binary", (op, x._cview(), y._cview(), out._view()), nbytes,
-                                 [out]))
+                    # Int32 / Int32 -> Float64 runs its own (compute-bound) kernel: its own class
+                    cls = "binary_" + kind + ("_div_i32" if out is o64 else "")
+                    jobs.append((cls, "binary", (op, x._cview(), y._cview(), out._view()), nbytes, [out]))
             mv = C_.mutable_view(slice(None), cu.R(None, None, -1), slice(None))
             jobs.append(("scatter", "copy", (mv._cview(), ap._cview()), 2 * n * es, [C_]))
         return jobs
@@ -680,7 +681,7 @@ def main():
     p.add_argument("--no-extra", action="store_true")
     p.add_argument("--profile-class", default=None,
                    help="run only one operation class (gather_permute, gather_reverse, binary_permute, "
-                        "binary_reverse, scatter) for profiling")
+                        "binary_reverse, binary_permute_div_i32, binary_reverse_div_i32, scatter) for profiling")
     p.add_argument("--profile-dtype", default="f32")
     p.add_argument("--profile-config", default=None, choices=["c3", "c4"],
                    help="one untimed pass of the fused-chain/reduction (c3) or heat (c4) workload, for profiling")
