@@ -449,7 +449,8 @@ def e2e_leg(A, lib, arrays, dev_arrays, jobs, args, timer, stop, step_bytes):
         lib.phcu_host_free(h)
     return {"value": round(step_bytes / (ms * 1e-3) / 1e9, 1), "unit": "GB/s", "ms_per_step": round(ms, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": steps,
-            "path": "phcu_upload_async/phcu_copy/phcu_binary/phcu_download_async/phcu_transfer_wait on pinned host buffers"}
+            "path": ("phcu_upload_async/phcu_copy/phcu_binary/phcu_download_async/phcu_transfer_wait "
+                     "on pinned host buffers")}
 
 
 # --------------------------------------------------------- other configs

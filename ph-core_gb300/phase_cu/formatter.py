@@ -296,7 +296,8 @@ def _compact_on_device(arr, ranges):
             soff += a * stride[d]
             doff += pos * ostride[d]
             bshape.append(b - a)
-        _copy_into(_make_view(out._buf, arr.dtype, doff, bshape, ostride), _make_view(buf, arr.dtype, soff, bshape, stride))
+        _copy_into(_make_view(out._buf, arr.dtype, doff, bshape, ostride),
+                   _make_view(buf, arr.dtype, soff, bshape, stride))
     return out
 
 
