@@ -84,9 +84,9 @@ __global__ void __launch_bounds__(HEAT_COLS) heat_step_kernel(const T* __restric
 // left-to-right infix chain as the one-step kernel on the same inputs, so the
 // result is bit-identical to ksteps single steps; the grid's boundary cells
 // copy themselves each step, and cells outside the grid (zero in the halo)
-// never reach an exact cell.  Warps walk rows; each lane takes four
-// consecutive cells of the row with vector accesses (a warp covers the whole
-// 128-cell shared row: no bank conflicts).
+// never reach an exact cell.  Each warp walks its own band of rows; each lane
+// takes four consecutive cells of a row with vector accesses (a warp covers
+// the whole 128-cell shared row: no bank conflicts).
 constexpr int HEAT_K = 4;
 constexpr int HEAT_SR = 72, HEAT_SC = 128;  // shared tile: rows x columns
 constexpr int HEAT_TR = HEAT_SR - 2 * HEAT_K, HEAT_TC = HEAT_SC - 2 * HEAT_K;  // 64 x 120 written
@@ -139,38 +139,53 @@ __global__ void __launch_bounds__(HEAT_BLOCK_THREADS) heat_block_kernel(const T*
   __syncthreads();
   T* src = buf0;
   T* dst = buf1;
+  // each warp walks a band of consecutive rows, keeping the row above and its
+  // current row in registers: one shared-memory row load per row and step
+  // instead of three
+  constexpr int NWARP = HEAT_BLOCK_THREADS / 32;
+  constexpr int BAND = (HEAT_SR - 2 + NWARP - 1) / NWARP;
+  const int rb = 1 + warp * BAND;
+  const int re = min(rb + BAND, HEAT_SR - 1);
   for (int s = 0; s < ksteps; s++) {
     // rows 1 .. HEAT_SR - 2 (the outer rows have no neighbours); the outer
     // columns are computed from the neighbouring rows' ends and never read back
     // as exact values
-    for (int r = 1 + warp; r < HEAT_SR - 1; r += HEAT_BLOCK_THREADS / 32) {
-      const int64_t i = i0 + r;
-      const bool row_int = i > 0 && i < n - 1;
-      const int b = r * HEAT_SC + 4 * lane;
-      T up[4], cv[4], dn[4], res[4];
-      heat_ld4(src + b - HEAT_SC, up);
-      heat_ld4(src + b, cv);
-      heat_ld4(src + b + HEAT_SC, dn);
-      // the neighbouring lanes' end cells; lanes 0 and 31 hold the tile's outer
-      // columns, whose results are never exact, so their wrapped values do not matter
-      const T lft = __shfl_up_sync(0xffffffffu, cv[3], 1);
-      const T rgt = __shfl_down_sync(0xffffffffu, cv[0], 1);
+    if (rb < re) {
+      T up[4], cv[4];
+      heat_ld4(src + (rb - 1) * HEAT_SC + 4 * lane, up);
+      heat_ld4(src + rb * HEAT_SC + 4 * lane, cv);
+      for (int r = rb; r < re; r++) {
+        const int64_t i = i0 + r;
+        const bool row_int = i > 0 && i < n - 1;
+        const int b = r * HEAT_SC + 4 * lane;
+        T dn[4], res[4];
+        heat_ld4(src + b + HEAT_SC, dn);
+        // the neighbouring lanes' end cells; lanes 0 and 31 hold the tile's outer
+        // columns, whose results are never exact, so their wrapped values do not matter
+        const T lft = __shfl_up_sync(0xffffffffu, cv[3], 1);
+        const T rgt = __shfl_down_sync(0xffffffffu, cv[0], 1);
 #pragma unroll
-      for (int e = 0; e < 4; e++) {
-        const T left = e == 0 ? lft : cv[e - 1];
-        const T right = e == 3 ? rgt : cv[e + 1];
-        res[e] = cv[e];
-        if (row_int && col_int[e]) {
-          T lap = up[e] + dn[e];
-          lap = lap + left;
-          lap = lap + right;
-          const T c4 = cv[e] * (T)4;
-          lap = lap - c4;
-          const T d = lap * coef;
-          res[e] = cv[e] + d;
+        for (int e = 0; e < 4; e++) {
+          const T left = e == 0 ? lft : cv[e - 1];
+          const T right = e == 3 ? rgt : cv[e + 1];
+          res[e] = cv[e];
+          if (row_int && col_int[e]) {
+            T lap = up[e] + dn[e];
+            lap = lap + left;
+            lap = lap + right;
+            const T c4 = cv[e] * (T)4;
+            lap = lap - c4;
+            const T d = lap * coef;
+            res[e] = cv[e] + d;
+          }
+        }
+        heat_st4(dst + b, res);
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+          up[e] = cv[e];
+          cv[e] = dn[e];
         }
       }
-      heat_st4(dst + b, res);
     }
     __syncthreads();
     T* t = src;
