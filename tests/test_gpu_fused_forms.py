@@ -1,8 +1,8 @@
 """Fused programs made only of pre-decoded operator forms (the reduced
 interpreter): every Float32 and Int32 form, operands swapped by a scalar on
 the left, Int32 immediates of Float32 operators, three and four inputs,
-checked Int32 overflow, on ROW (reversed view) and tile (permuted view)
-launches.  Each chain is checked against the oracle applied one reference
+checked Int32 overflow, on ROW (reversed view), TMA tile (permuted view) and
+staged tile (permuted view of an odd shape) launches.  Each chain is checked against the oracle applied one reference
 operation at a time."""
 import numpy as np
 import pytest
@@ -10,6 +10,9 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 SHAPE = [24, 40, 36]
+# an odd innermost length: the permuted view's strides are not 16-byte
+# multiples, so its tiles are staged without the Tensor Memory Accelerator
+ODD_SHAPE = [24, 40, 37]
 
 
 def _view(cu, X, kind):
@@ -18,14 +21,18 @@ def _view(cu, X, kind):
     return X.view().permute(2, 0, 1)
 
 
+def _shape(kind):
+    return ODD_SHAPE if kind == "permute_odd" else SHAPE
+
+
 def _host(x, kind):
     return np.ascontiguousarray(x[:, ::-1, :] if kind == "reverse" else np.transpose(x, (2, 0, 1)))
 
 
-@pytest.mark.parametrize("kind", ["reverse", "permute"])
+@pytest.mark.parametrize("kind", ["reverse", "permute", "permute_odd"])
 def test_float32_forms(cu, ora, kind):
     rng = np.random.default_rng(2)
-    a, b, c, d = [(rng.standard_normal(SHAPE) * 5).astype(np.float32) for _ in range(4)]
+    a, b, c, d = [(rng.standard_normal(_shape(kind)) * 5).astype(np.float32) for _ in range(4)]
     A, B, C, D = (_view(cu, cu.CuNArray.from_numpy(x), kind) for x in (a, b, c, d))
     ha, hb, hc, hd = (_host(x, kind) for x in (a, b, c, d))
     # ((a + 3) * b - c) / d, then 2.5f - acc, then 0.75f / acc, then + a
@@ -53,10 +60,10 @@ def test_float32_forms(cu, ora, kind):
     assert np.array_equal(pw.to_narr(), t)
 
 
-@pytest.mark.parametrize("kind", ["reverse", "permute"])
+@pytest.mark.parametrize("kind", ["reverse", "permute", "permute_odd"])
 def test_int32_forms(cu, ora, kind):
     rng = np.random.default_rng(3)
-    a, b, c, d = [rng.integers(-1000, 1000, SHAPE).astype(np.int32) for _ in range(4)]
+    a, b, c, d = [rng.integers(-1000, 1000, _shape(kind)).astype(np.int32) for _ in range(4)]
     A, B, C, D = (_view(cu, cu.CuNArray.from_numpy(x), kind) for x in (a, b, c, d))
     ha, hb, hc, hd = (_host(x, kind) for x in (a, b, c, d))
     pv = (((((A.process(lambda e: e + 7) * B) - C).__rsub__(5)).wadd(D).wmul(B).wsub(C) & A) | B) ^ D
