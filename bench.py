@@ -382,8 +382,9 @@ def e2e_leg(A, lib, arrays, dev_arrays, jobs, args, timer, stop, step_bytes):
     every result downloaded inside the timed region.  Each operation writes its
     own device output; the uploads run on the library's host-to-device stream,
     every download starts behind its operation (phcu_download_async) into one
-    of two pinned staging buffers and overlaps the operations after it, and a
-    step ends when all its results are on the host (phcu_transfer_wait)."""
+    of two pinned staging buffers and overlaps the operations after it, and the
+    next step's uploads overlap this step's last downloads; every step uploads
+    its inputs and downloads all its results inside the timed region."""
     import phase_cu as cu
 
     def pinned(nbytes):
@@ -419,26 +420,37 @@ def e2e_leg(A, lib, arrays, dev_arrays, jobs, args, timer, stop, step_bytes):
     staging = [pinned(staging_bytes), pinned(staging_bytes)]
     own = [(k, a_, t_, staging[i % 2], m_) for i, (k, a_, t_, _, m_) in enumerate(own)]
 
-    def one_step(dev_arrays):
+    def upload(dev_arrays):
         for dt in ("f32", "i32"):
             pa, pb, nb = host_in[dt]
             Ad, Bd, _ = dev_arrays[dt]
             A.check(lib.phcu_upload_async(Ad._buf.ptr, pa, nb))
             A.check(lib.phcu_upload_async(Bd._buf.ptr, pb, nb))
-        for kind, a, target, hbuf, _ in own:
-            if kind == "copy":
-                A.check(lib.phcu_copy(ctypes.byref(a[0]), ctypes.byref(a[1])))
-            else:
-                A.check(lib.phcu_binary(a[0], ctypes.byref(a[1]), ctypes.byref(a[2]), ctypes.byref(a[3])))
-            A.check(lib.phcu_download_async(hbuf, target._buf.ptr, target._buf.nbytes))
+
+    def run_steps(dev_arrays, n):
+        # Step k's uploads are issued right after step k-1's operations, so they
+        # run on the host-to-device engine while step k-1's results are still
+        # being downloaded (phcu_upload_async waits for the kernels that read the
+        # inputs).  The wait before step k's operations covers those uploads and
+        # step k-1's downloads, whose device buffers step k overwrites.
+        upload(dev_arrays)
+        for k in range(n):
+            A.check(lib.phcu_transfer_wait())
+            for kind, a, target, hbuf, _ in own:
+                if kind == "copy":
+                    A.check(lib.phcu_copy(ctypes.byref(a[0]), ctypes.byref(a[1])))
+                else:
+                    A.check(lib.phcu_binary(a[0], ctypes.byref(a[1]), ctypes.byref(a[2]), ctypes.byref(a[3])))
+                A.check(lib.phcu_download_async(hbuf, target._buf.ptr, target._buf.nbytes))
+            if k + 1 < n:
+                upload(dev_arrays)
         A.check(lib.phcu_transfer_wait())
 
-    one_step(dev_arrays)
+    run_steps(dev_arrays, 1)
     A.call("phcu_sync")
     steps = max(1, min(args.steps, 5))
     t = timer()
-    for _ in range(steps):
-        one_step(dev_arrays)
+    run_steps(dev_arrays, steps)
     ms = stop(t) / steps
     h2d = sum(2 * v[2] for v in host_in.values())
     d2h = sum(x[2]._buf.nbytes for x in own)
