@@ -5,7 +5,7 @@ autotune, phcu_tune_measure).  `MLP` is the 24 -> 64 -> 64 -> 1 network whose
 forward, backward and Adam steps run on the GPU (phcu_mlp_*); it is trained
 to predict log2(time) of (task, configuration) from `features`, and `pick`
 chooses, per task, the configuration with the smallest predicted time.  The
-exhaustive timings stay the judge: `regret` compares any choice with the best
+exhaustive timings remain the yardstick: `regret` compares any choice with the best
 measured configuration.
 """
 import ctypes
