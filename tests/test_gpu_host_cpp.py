@@ -1,0 +1,129 @@
+"""The C++ host mirror (ph-core_gb300/host/phase.hpp) on the device: views,
+infix operators with Crystal's result types, reductions, chunk reads and
+writes and the reference's exceptions, checked against the oracle on
+16x12x10 Float32 and Int32 arrays (bit-exact; sums within 1e-6 relative of
+the FP64 oracle)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SHAPE = (16, 12, 10)
+
+
+def _cuda_lib_dir():
+    """The directory holding libcudart.so of the toolkit nvcc belongs to."""
+    import glob
+
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    home = os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    for d in [os.path.join(home, "lib64")] + sorted(glob.glob(os.path.join(home, "targets", "*", "lib"))):
+        if os.path.exists(os.path.join(d, "libcudart.so")):
+            return d
+    return os.path.join(home, "lib64")
+
+
+@pytest.fixture(scope="module")
+def run(tmp_path_factory, cu):
+    from phase_cu import synth
+
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("hostcpp_dev")
+    lib = os.path.join(ROOT, "ph-core_gb300", "phase_cu", "_lib")
+    exe = str(d / "host_cpp_device")
+    cmd = [gxx, "-std=c++17", "-O1", "-o", exe, os.path.join(ROOT, "tests", "host_cpp_device.cpp"),
+           "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "ph-core_gb300", "host"),
+           "-L", lib, "-lphcuda", "-Wl,-rpath," + lib, "-L", _cuda_lib_dir(), "-Wl,-rpath," + _cuda_lib_dir()]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    n = int(np.prod(SHAPE))
+    arrays = {
+        "f32": (synth.uniform_f32(list(SHAPE), seed=4), synth.uniform_f32(list(SHAPE), seed=4, start=n)),
+        "i32": (synth.uniform_i32(list(SHAPE), seed=4, lo=-1000, hi=1000),
+                synth.uniform_i32(list(SHAPE), seed=4, lo=-1000, hi=1000, start=n)),
+    }
+    for tag, (a, b) in arrays.items():
+        a.tofile(str(d / ("a." + tag)))
+        b.tofile(str(d / ("b." + tag)))
+    p = subprocess.run([exe, str(d)], capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stdout[-2000:] + p.stderr[-2000:]
+    lines = p.stdout.splitlines()
+
+    def load(name, dtype):
+        return np.fromfile(str(d / (name + ".bin")), dtype=dtype)
+
+    return arrays, lines, load
+
+
+@pytest.mark.parametrize("tag", ["f32", "i32"])
+def test_views_operators_and_chunks(run, ora, cu, tag):
+    arrays, lines, load = run
+    a, b = arrays[tag]
+    dt = a.dtype
+    perm, rev = [("permute", [2, 0, 1])], [("region", [slice(None), cu.R(None, None, -1), slice(None)])]
+    oap, obp = ora.ViewOperand(a, perm), ora.ViewOperand(b, perm)
+    oar, obr = ora.ViewOperand(a, rev), ora.ViewOperand(b, rev)
+    assert np.array_equal(load(tag + "_perm", dt), ora.gather(oap).reshape(-1))
+    assert np.array_equal(load(tag + "_rev", dt), ora.gather(oar).reshape(-1))
+    assert np.array_equal(load(tag + "_add_perm", dt), ora.map_binary(ora.OP_ADD, oap, obp)[0].reshape(-1))
+    assert np.array_equal(load(tag + "_sub_rev", dt), ora.map_binary(ora.OP_SUB, oar, obr)[0].reshape(-1))
+    div = ora.map_binary(ora.OP_DIV, oap, obp)[0]
+    assert div.dtype == (np.float32 if tag == "f32" else np.float64)  # Int32 / Int32 is Float64
+    assert np.array_equal(load(tag + "_div_perm", div.dtype), div.reshape(-1), equal_nan=True)
+    mul_op = ora.OP_MUL if tag == "f32" else ora.OP_WMUL
+    assert np.array_equal(load(tag + "_mul_rev", dt), ora.map_binary(mul_op, oar, obr)[0].reshape(-1))
+    t, _ = ora.map_binary_scalar(ora.OP_MUL, ora.gather(oap), dt.type(3), ora.F32 if tag == "f32" else ora.I32)
+    t, _ = ora.map_binary_scalar(ora.OP_SUB, t, dt.type(7), ora.F32 if tag == "f32" else ora.I32, scalar_left=True)
+    assert np.array_equal(load(tag + "_scal", dt), t.reshape(-1))
+    chunk = ora.narray_fetch_chunk(a, [1, cu.R(0, 10, 3, True), cu.R(-1, 2)])
+    assert chunk.shape == (4, 8)
+    assert np.array_equal(load(tag + "_chunk", dt), chunk.reshape(-1))
+    c = np.full([10, 16, 12], 5, dtype=dt)
+    od = ora.ViewOperand(c, rev)
+    ora.scatter(od, oap)
+    c = od.arr
+    c[2, 0:4, :] = -1
+    assert np.array_equal(load(tag + "_scatter", dt), c.reshape(-1))
+    for name, exc in (("_shape", "ShapeError"), ("_index", "IndexError"), ("_dim", "DimensionError")):
+        assert "raised %s%s %s" % (tag, name, exc) in lines
+
+
+@pytest.mark.parametrize("tag", ["f32", "i32"])
+def test_reductions(run, ora, tag):
+    arrays, _, load = run
+    a, _ = arrays[tag]
+    dt = a.dtype
+    ap = np.ascontiguousarray(np.transpose(a, (2, 0, 1)))
+    ar = np.ascontiguousarray(a[:, ::-1, :])
+    for k in range(3):
+        s = load(tag + "_sum%d" % k, dt)
+        if tag == "f32":
+            ref = ora.reduce_f64(ap, k).reshape(-1)
+            mag = ora.reduce_f64(np.abs(ap), k).reshape(-1)
+            assert np.all(np.abs(s - ref) <= 1e-6 * mag + 1e-30), k  # tolerance: 1e-6 of the sum of magnitudes
+        else:
+            assert np.array_equal(s, ora.reduce(ora.RED_SUM, ap, k).reshape(-1))
+        assert np.array_equal(load(tag + "_max%d" % k, dt), ora.reduce(ora.RED_MAX, ar, k).reshape(-1))
+        assert np.array_equal(load(tag + "_argmax%d" % k, np.int32),
+                              ora.reduce(ora.RED_ARGMAX, ap, k, ora.I32).reshape(-1))
+    full = load(tag + "_sumall", dt)[0]
+    ref = ora.reduce_f64(a)
+    if tag == "f32":
+        assert abs(full - ref) <= 1e-6 * float(np.abs(a.astype(np.float64)).sum())
+    else:
+        assert full == int(ref)
+    coord = load(tag + "_argmaxall", np.int64)
+    assert list(coord) == list(np.unravel_index(int(ora.reduce(ora.RED_ARGMAX, ar)), ar.shape))
+
+
+def test_checked_and_wrapping_int32(run):
+    _, lines, load = run
+    assert "raised overflow OverflowError" in lines
+    assert np.all(load("wrapped", np.int32) == np.int32(-2 ** 31))
