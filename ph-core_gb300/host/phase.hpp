@@ -240,6 +240,111 @@ struct IndexRegion {
     return r;
   }
 
+  // IndexRegion.new(region_literal, drop) without a bound (index_region.cr:255-283):
+  // negative indices have no meaning, and every range needs its far end.
+  static IndexRegion absolute(const std::vector<Lit>& lits, bool drop = true) {
+    IndexRegion r;
+    r.drop = drop;
+    for (const Lit& l : lits) {
+      if (l.is_index) {
+        if (l.index < 0) throw IndexError("Negative indices have no meaning when a bounding shape is not provided.");
+      } else {
+        if ((l.first && *l.first < 0) || (l.last && *l.last < 0))
+          throw IndexError("Negative indices have no meaning when a bounding shape is not provided.");
+        const bool bounded = (!l.step || *l.step >= 0) ? (bool)l.last : (bool)l.first;
+        if (!bounded)
+          throw ArgumentError("Cannot create IndexRegion without an explicit upper bound unless you provide a "
+                              "bounding shape");
+      }
+      r.axes.push_back(infer_range(l, 0));
+      r.degenerate.push_back(l.is_index);
+    }
+    return r;
+  }
+
+  // IndexRegion#fits_in? (index_region.cr:468-478).
+  bool fits_in(const std::vector<int64_t>& bound) const {
+    if (bound.size() != axes.size())
+      throw DimensionError("The bound shape provided had a different number of dimensions than this IndexRegion.");
+    for (size_t i = 0; i < axes.size(); i++)
+      if (bound[i] <= std::max(axes[i].first, axes[i].last)) return false;
+    return true;
+  }
+
+  // IndexRegion#trim! (index_region.cr:502-515, trim_axis :684-702).
+  IndexRegion& trim(const std::vector<int64_t>& bound) {
+    if (bound.size() != axes.size()) throw DimensionError("Cannot trim a region to a shape of another rank");
+    for (size_t a = 0; a < axes.size(); a++) {
+      AxisRange& x = axes[a];
+      const int64_t nb = bound[a], as = x.step < 0 ? -x.step : x.step;
+      if (x.first >= nb) {
+        if (x.last >= nb) {
+          x = {0, 0, 0, 0};
+        } else if (x.step < 0) {
+          int64_t span = (nb - 1) - x.last;
+          x.size = span / as + 1;
+          span -= span % as;
+          x.first = x.last + span;
+        }
+      } else if (x.step > 0 && x.last >= nb) {
+        int64_t span = (nb - 1) - x.first;
+        span -= span % as;
+        x.size = span / as + 1;
+        x.last = x.first + span;
+      }
+    }
+    return *this;
+  }
+
+  // IndexRegion#reverse! (index_region.cr:533-537).
+  IndexRegion& reverse() {
+    for (AxisRange& x : axes) {
+      std::swap(x.first, x.last);
+      x.step = -x.step;
+    }
+    return *this;
+  }
+
+  // IndexRegion#translate! (index_region.cr:577-585).
+  IndexRegion& translate(const std::vector<int64_t>& offset) {
+    for (size_t a = 0; a < offset.size() && a < axes.size(); a++)
+      if (offset[a] < 0 && (axes[a].first < -offset[a] || axes[a].last < -offset[a]))
+        throw IndexError("Can't translate to negative indices");
+    for (size_t a = 0; a < offset.size() && a < axes.size(); a++) {
+      axes[a].first += offset[a];
+      axes[a].last += offset[a];
+    }
+    return *this;
+  }
+
+  // IndexRegion#includes? (index_region.cr:445-458).
+  bool includes(const std::vector<int64_t>& coord) const {
+    if (coord.size() != axes.size()) return false;
+    for (size_t i = 0; i < axes.size(); i++) {
+      const AxisRange& x = axes[i];
+      const int64_t lo = x.step > 0 ? x.first : x.last, hi = x.step > 0 ? x.last : x.first;
+      if (coord[i] < lo || coord[i] > hi || x.step == 0) return false;
+      if ((coord[i] - x.first) % x.step != 0) return false;
+    }
+    return true;
+  }
+
+  // IndexRegion#local_to_absolute_unsafe (index_region.cr:621-637): a
+  // coordinate of the region's (reduced) shape to one of the bound shape.
+  std::vector<int64_t> local_to_absolute(const std::vector<int64_t>& coord) const {
+    std::vector<int64_t> out;
+    size_t la = 0;
+    for (size_t i = 0; i < axes.size(); i++) {
+      if (drop && degenerate[i]) {
+        out.push_back(axes[i].first);
+      } else {
+        out.push_back(axes[i].first + coord[la] * axes[i].step);
+        la++;
+      }
+    }
+    return out;
+  }
+
   // IndexRegion#shape (index_region.cr:304-317): the kept axes' sizes, or
   // [size] when every axis is dropped.
   std::vector<int64_t> shape() const {

@@ -1,7 +1,9 @@
 """The C++ host mirror (ph-core_gb300/host/phase.hpp): its RangeSyntax /
-IndexRegion canonicalisation against the reference's TestRanges and region
-KATs, and against the Python mirror (itself pinned by those KATs) on 3,000
-random region literals.  Host logic only: compiled with g++, no GPU."""
+IndexRegion logic (canonicalisation, absolute regions, fits_in?, trim!,
+reverse!, translate!, includes?, local_to_absolute) against the reference's
+TestRanges and IndexRegion KATs, and against the Python mirror (itself pinned
+by those KATs) on 3,000 random regions and operations.  Host logic only:
+compiled with g++, no GPU."""
 import os
 import random
 import shutil
@@ -32,29 +34,56 @@ def _tok(v):
     return "n" if v is None else str(int(v))
 
 
-def _encode(bound, lits):
-    parts = [str(len(bound))] + [str(b) for b in bound] + [str(len(lits))]
+def _ints(v):
+    return [str(len(v))] + [str(int(x)) for x in v]
+
+
+def _encode(bound, lits, op=("none",)):
+    """bound None = an absolute region (no bounding shape)."""
+    parts = ["A"] if bound is None else ["N", str(len(bound))] + [str(b) for b in bound]
+    parts.append(str(len(lits)))
     for x in lits:
         if isinstance(x, int):
             parts += ["I", str(x)]
         else:
             parts += ["R", _tok(x.first), _tok(x.last), _tok(x.step), "1" if x.exclusive else "0"]
+    parts.append(op[0])
+    if len(op) > 1:
+        parts += _ints(op[1])
     return " ".join(parts)
 
 
-def _python(bound, lits):
-    try:
-        r = reg.IndexRegion.new(lits, bound)
-    except DimensionError:
-        return "ERR DimensionError"
-    except IndexError:
-        return "ERR IndexError"
+def _region_text(r):
     axes = " ".join("%d %d %d %d" % t for t in zip(r.first, r.step, r.last, r.proper_shape))
     return "OK %d %s | %s" % (len(r.shape), " ".join(str(v) for v in r.shape), axes)
 
 
+def _python(bound, lits, op=("none",)):
+    try:
+        r = reg.IndexRegion.absolute(lits) if bound is None else reg.IndexRegion.new(lits, bound)
+        if op[0] == "fits":
+            return "BOOL %d" % r.fits_in(op[1])
+        if op[0] == "incl":
+            return "BOOL %d" % r.includes(op[1])
+        if op[0] == "l2a":
+            return "COORD " + " ".join(str(v) for v in r.local_to_absolute(op[1]))
+        if op[0] == "trim":
+            r.trim(op[1])
+        elif op[0] == "rev":
+            r.reverse()
+        elif op[0] == "trans":
+            r.translate(op[1])
+        return _region_text(r)
+    except DimensionError:
+        return "ERR DimensionError"
+    except IndexError:
+        return "ERR IndexError"
+    except ValueError:
+        return "ERR ArgumentError"
+
+
 def _run(exe, cases):
-    text = "\n".join(_encode(b, l) for b, l in cases) + "\n"
+    text = "\n".join(_encode(*c) for c in cases) + "\n"
     out = subprocess.run([exe], input=text, capture_output=True, text=True, check=True).stdout.splitlines()
     assert len(out) == len(cases)
     return [" ".join(o.split()) for o in out]
@@ -76,18 +105,44 @@ def test_test_ranges_kats(exe, kats):
     assert all(o == "ERR IndexError" for o in _run(exe, [([b], [_lit(lit)]) for lit in bad]))
     for o in _run(exe, [([b], [_lit(lit)]) for lit in tr["empty"]]):
         assert o.startswith("OK 1 0 |"), o
+    # absolute regions (spec/spec_helper.cr TestRanges without a bound)
+    out = _run(exe, [(None, [_lit(lit)]) for lit, _ in tr["fully_defined"]])
+    for (lit, (f, s, l)), o in zip(tr["fully_defined"], out):
+        assert o.split("|")[1].split()[:3] == [str(f), str(s), str(l)], (lit, o)
+    assert all(o.startswith("ERR") for o in _run(exe, [(None, [_lit(lit)]) for lit, _ in tr["implicit_bounds"]]))
+    assert all(o == "ERR IndexError" for o in _run(exe, [(None, [_lit(lit)]) for lit, _ in tr["negative_indices"]]))
 
 
-def test_region_multi_axis_kat(exe, kats):
+def test_index_region_kats(exe, kats):
     k = kats["region_multi_axis"]
-    o = _run(exe, [(k["bound"], [_lit(x) for x in k["literal"]]),
-                   (k["bound"], [_lit(x) for x in k["bad_literal"]])])
+    o = _run(exe, [(k["bound"], [_lit(x) for x in k["literal"]]), (k["bound"], [_lit(x) for x in k["bad_literal"]])])
     axes = " ".join("%d %d %d %d" % t for t in zip(k["first"], k["step"], k["last"], k["shape"]))
     assert o[0] == "OK 2 %s | %s" % (" ".join(map(str, k["shape"])), axes)
     assert o[1] == "ERR IndexError"
+    k = kats["region_absolute"]
+    o = _run(exe, [(None, [_lit(x) for x in k["literal"]])])[0]
+    axes = " ".join("%d %d %d %d" % t for t in zip(k["first"], k["step"], k["last"], k["shape"]))
+    assert o == "OK 2 %s | %s" % (" ".join(map(str, k["shape"])), axes)
+    k = kats["region_includes"]
+    lits = [_lit(x) for x in k["literal"]]
+    assert all(o == "BOOL 1" for o in _run(exe, [(None, lits, ("incl", c)) for c in k["included"]]))
+    assert all(o == "BOOL 0" for o in _run(exe, [(None, lits, ("incl", c)) for c in k["excluded"]]))
+    k = kats["region_fits_in"]
+    lits = [_lit(x) for x in k["literal"]]
+    assert all(o == "BOOL 1" for o in _run(exe, [(None, lits, ("fits", b)) for b in k["fits"]]))
+    assert all(o == "BOOL 0" for o in _run(exe, [(None, lits, ("fits", b)) for b in k["not_fits"]]))
+    k = kats["region_translate"]
+    lits = [_lit(x) for x in k["literal"]]
+    base, moved = _run(exe, [(None, lits), (None, lits, ("trans", k["offset"]))])
+    firsts = lambda o: [int(v) for v in o.split("|")[1].split()[0::4]]  # noqa: E731
+    assert firsts(moved) == [f + d for f, d in zip(firsts(base), k["offset"])]
+    assert all(o == "ERR IndexError" for o in _run(exe, [(None, lits, ("trans", off)) for off in k["raises"]]))
+    k = kats["region_reverse"]
+    o = _run(exe, [(None, [_lit(x) for x in k["literal"]], ("rev",))])[0]
+    assert firsts(o) == k["first_after"]
 
 
-def test_random_literals_match_the_python_mirror(exe):
+def test_random_regions_and_operations_match_the_python_mirror(exe):
     rnd = random.Random(5)
     cases = []
     for _ in range(3000):
@@ -101,7 +156,26 @@ def test_random_literals_match_the_python_mirror(exe):
                 pick = lambda: None if rnd.random() < 0.3 else rnd.randint(-14, 14)  # noqa: E731
                 step = None if rnd.random() < 0.4 else rnd.choice([-3, -2, -1, 1, 2, 3])
                 lits.append(reg.R(pick(), pick(), step, rnd.random() < 0.3))
-        cases.append((bound, lits))
+        kind = rnd.choice(["none", "rev", "trim", "trans", "incl", "fits", "l2a"])
+        n = rank if rnd.random() < 0.9 else rank + 1
+        if kind in ("trim", "fits"):
+            op = (kind, [rnd.randint(0, 14) for _ in range(n)])
+        elif kind == "trans":
+            op = (kind, [rnd.randint(-4, 4) for _ in range(rank)])
+        elif kind == "incl":
+            op = (kind, [rnd.randint(-1, 13) for _ in range(n)])
+        elif kind == "l2a":
+            try:
+                shape = reg.IndexRegion.new(lits, bound).shape
+            except (IndexError, DimensionError):
+                shape = []
+            if not shape or min(shape) == 0:
+                op = ("none",)
+            else:
+                op = (kind, [rnd.randint(0, s - 1) for s in shape])
+        else:
+            op = (kind,)
+        cases.append((bound, lits, op))
     out = _run(exe, cases)
-    for (bound, lits), o in zip(cases, out):
-        assert o == " ".join(_python(bound, lits).split()), (bound, lits, o)
+    for (bound, lits, op), o in zip(cases, out):
+        assert o == " ".join(_python(bound, lits, op).split()), (bound, lits, op, o)
