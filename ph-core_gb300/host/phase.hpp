@@ -56,6 +56,12 @@ struct EmptyError : PhaseError {
 struct DeviceError : PhaseError {
   using PhaseError::PhaseError;
 };
+// A fused expression the device program cannot hold (more than
+// PHCU_MAX_INPUTS distinct views, PHCU_MAX_INSTR instructions or two nested
+// stashes), or an operator Crystal does not define for the operand types.
+struct NotImplementedError : PhaseError {
+  using PhaseError::PhaseError;
+};
 
 inline std::string last_error() {
   char buf[512];
@@ -457,6 +463,8 @@ inline Affine affine_reverse(const Affine& a) {
 
 template <typename T>
 class CuNArray;
+template <typename T>
+class CuProcView;
 
 // A strided, aliasing view of an array (src/view.cr): region, permute and
 // reverse rewrite the layout; materialising takes one gather kernel.
@@ -488,6 +496,13 @@ class CuView {
   // View#to_narr (view.cr:123-126): one gather into a new contiguous array.
   CuNArray<T> to_cu() const;
   std::vector<T> to_vector() const;
+
+  // MultiIndexable#process (view.cr:119-121, proc_view.cr:6-35): a lazy
+  // elementwise program over this view; f maps a Sym<T> to a Sym<R> (or a
+  // constant).  Nothing runs until the result is materialised.
+  CuProcView<T> process() const;
+  template <typename F>
+  auto process(F f) const;
 
  protected:
   std::shared_ptr<Buffer> buf_;
@@ -540,6 +555,9 @@ class CuNArray : public CuView<T> {
     check(phcu_copy(&d, &s), "phcu_copy");
   }
   void set_chunk(const std::vector<Lit>& region, T value) { fill_view(this->view(region).desc(), value); }
+  // A fused source is materialised first (it may read the region it writes,
+  // as the heat step does), then copied in.
+  void set_chunk(const std::vector<Lit>& region, const CuProcView<T>& src) { set_chunk(region, src.to_cu()); }
 
  private:
   static int64_t count(const std::vector<int64_t>& shape) {
@@ -650,6 +668,482 @@ CuNArray<T> wsub(const CuView<T>& a, const CuView<T>& b) { return detail::binary
 template <typename T>
 CuNArray<T> wmul(const CuView<T>& a, const CuView<T>& b) { return detail::binary<T>(PHCU_OP_WMUL, a, b); }
 
+// ---------------------------------------------------- fused expressions
+// ProcView (src/proc_view.cr:6-35) and chained infix operators build an
+// expression over up to PHCU_MAX_INPUTS aliasing views; materialising it
+// compiles the expression into the library's accumulator program
+// (phcu_program_t) and runs ONE phcu_eval, instead of the reference's one
+// map_with pass per operator (multi_indexable.cr:1026-1078).
+namespace detail {
+constexpr bool is_int_type(int32_t t) { return t == PHCU_I32 || t == PHCU_I64; }
+constexpr bool is_float_type(int32_t t) { return t == PHCU_F32 || t == PHCU_F64; }
+
+// Crystal's result type of `a op b` for numeric operands (Number#+ and
+// friends; Int / Int is Float64, Int ** Float is Float64), or -1 where
+// Crystal defines no such operator (bitwise or wrapping operators on floats).
+constexpr int32_t result_type(int32_t op, int32_t ta, int32_t tb) {
+  if (op == PHCU_OP_GT || op == PHCU_OP_LT || op == PHCU_OP_GE || op == PHCU_OP_LE || op == PHCU_OP_EQ)
+    return PHCU_BOOL;
+  if (op == PHCU_OP_CMP) return PHCU_I32;
+  if (op == PHCU_OP_AND || op == PHCU_OP_OR || op == PHCU_OP_XOR)
+    return is_int_type(ta) && is_int_type(tb) ? ta : -1;
+  if (is_int_type(ta) && is_int_type(tb)) return op == PHCU_OP_DIV ? PHCU_F64 : ta;
+  if (op == PHCU_OP_WADD || op == PHCU_OP_WSUB || op == PHCU_OP_WMUL || op == PHCU_OP_WPOW) return -1;
+  if (is_int_type(ta) && is_float_type(tb) && op == PHCU_OP_POW) return PHCU_F64;
+  return ta == PHCU_F64 || tb == PHCU_F64 ? PHCU_F64 : PHCU_F32;
+}
+
+// The type an instruction computes in: Float32 ** Int keeps the float and
+// takes an integer exponent (repeated squaring, x ** 2 == x * x).
+constexpr int32_t compute_type(int32_t op, int32_t ta, int32_t tb) {
+  if (is_int_type(ta) && is_int_type(tb)) return ta;
+  if (op == PHCU_OP_POW && is_float_type(ta) && is_int_type(tb)) return ta;
+  if (is_int_type(ta) && is_float_type(tb) && op == PHCU_OP_POW) return PHCU_F64;
+  return ta == PHCU_F64 || tb == PHCU_F64 ? PHCU_F64 : PHCU_F32;
+}
+
+// Operators whose kernel may set the status word: checked Int arithmetic
+// (OverflowError, DivisionByZeroError, negative exponents) and `%`.
+constexpr bool program_can_raise(int32_t op, int32_t ta, int32_t tb) {
+  if (is_int_type(ta) && is_int_type(tb))
+    return op == PHCU_OP_ADD || op == PHCU_OP_SUB || op == PHCU_OP_MUL || op == PHCU_OP_FLOORDIV ||
+           op == PHCU_OP_MOD || op == PHCU_OP_POW || op == PHCU_OP_WPOW;
+  return op == PHCU_OP_MOD;
+}
+
+// One node of an expression tree.
+struct Expr {
+  enum Kind { IN, CONST, BIN, UN } kind = IN;
+  int32_t op = 0;          // BIN: PHCU_OP_*; UN: PHCU_I_NEG / PHCU_I_NOT / PHCU_I_POS
+  int32_t t = 0;           // type of the node's value
+  int32_t ta = 0, tb = 0;  // BIN: types of the operands
+  int32_t slot = 0;        // IN: input slot
+  int64_t bits = 0;        // CONST: the value's bit pattern in a program slot
+  std::shared_ptr<const Expr> a, b;
+};
+using ExprP = std::shared_ptr<const Expr>;
+
+inline ExprP input(int32_t slot, int32_t t) {
+  auto e = std::make_shared<Expr>();
+  e->kind = Expr::IN;
+  e->slot = slot;
+  e->t = t;
+  return e;
+}
+
+// The bit pattern of a constant in a 64-bit program slot: Float32 and Int32
+// fill the low 32 bits (the rest zero), Float64 and Int64 all 64.
+inline int64_t slot_bits(float v) {
+  uint32_t u;
+  std::memcpy(&u, &v, 4);
+  return (int64_t)u;
+}
+inline int64_t slot_bits(double v) {
+  int64_t u;
+  std::memcpy(&u, &v, 8);
+  return u;
+}
+inline int64_t slot_bits(int32_t v) { return (int64_t)(uint32_t)v; }
+inline int64_t slot_bits(int64_t v) { return v; }
+
+template <typename S>
+ExprP constant(S v) {
+  auto e = std::make_shared<Expr>();
+  e->kind = Expr::CONST;
+  e->t = DType<S>::id;
+  e->bits = slot_bits(v);
+  return e;
+}
+
+inline ExprP binary_expr(int32_t op, ExprP a, ExprP b) {
+  const int32_t t = result_type(op, a->t, b->t);
+  if (t < 0) throw NotImplementedError("the operator is not defined for these operand types");
+  auto e = std::make_shared<Expr>();
+  e->kind = Expr::BIN;
+  e->op = op;
+  e->ta = a->t;
+  e->tb = b->t;
+  e->t = t;
+  e->a = std::move(a);
+  e->b = std::move(b);
+  return e;
+}
+
+inline ExprP unary_expr(int32_t op, ExprP a) {
+  auto e = std::make_shared<Expr>();
+  e->kind = Expr::UN;
+  e->op = op;
+  e->t = a->t;
+  e->a = std::move(a);
+  return e;
+}
+
+// The same tree with every input slot k replaced by map(k).
+template <typename M>
+ExprP relabel(const ExprP& e, const M& map) {
+  if (e->kind == Expr::CONST) return e;
+  auto n = std::make_shared<Expr>(*e);
+  if (e->kind == Expr::IN) n->slot = map(e->slot);
+  if (e->a) n->a = relabel(e->a, map);
+  if (e->b) n->b = relabel(e->b, map);
+  return n;
+}
+
+// Expression tree -> accumulator program.  Leaves (an input or a constant)
+// become operand B of an instruction; a binary node whose operands are both
+// compound evaluates the right one first into a stash register (S0, then S1
+// one level deeper), so a program needs no stack.
+class ProgramCompiler {
+ public:
+  phcu_program_t prog;
+  bool raises = false;
+
+  ProgramCompiler() { std::memset(&prog, 0, sizeof(prog)); }
+
+  void run(const ExprP& e, int32_t out_type) {
+    gen(*e, 0);
+    if (e->t != out_type) emit(PHCU_I_CVT, 0, e->t, 0, out_type);
+    prog.out_type = out_type;
+  }
+
+ private:
+  void emit(int32_t op, int32_t src, int32_t t, int32_t bt, int64_t imm, int32_t flags = 0) {
+    if (prog.n_instr >= PHCU_MAX_INSTR)
+      throw NotImplementedError("fused program longer than " + std::to_string(PHCU_MAX_INSTR) + " instructions");
+    phcu_instr_t& c = prog.code[prog.n_instr++];
+    c.op = (uint8_t)op;
+    c.src = (uint8_t)src;
+    c.type = (uint8_t)t;
+    c.btype = (uint8_t)bt;
+    c.flags = (uint8_t)flags;
+    c.imm.i = imm;
+  }
+  static bool leaf(const Expr& e) { return e.kind == Expr::IN || e.kind == Expr::CONST; }
+  static int32_t src_of(const Expr& e) { return e.kind == Expr::IN ? e.slot : PHCU_SRC_IMM; }
+  static int64_t imm_of(const Expr& e) { return e.kind == Expr::IN ? 0 : e.bits; }
+
+  void gen(const Expr& e, int depth) {
+    if (leaf(e)) {
+      emit(PHCU_I_LD, src_of(e), e.t, e.t, imm_of(e));
+      return;
+    }
+    if (e.kind == Expr::UN) {
+      gen(*e.a, depth);
+      if (e.op == PHCU_I_NEG && is_int_type(e.t)) raises = true;
+      emit(e.op, 0, e.t, 0, 0);
+      return;
+    }
+    const Expr& l = *e.a;
+    const Expr& r = *e.b;
+    const int32_t T = compute_type(e.op, e.ta, e.tb);
+    if (program_can_raise(e.op, e.ta, e.tb)) raises = true;
+    if (leaf(r)) {
+      gen(l, depth);
+      if (e.ta != T) emit(PHCU_I_CVT, 0, e.ta, 0, T);
+      emit(e.op, src_of(r), T, r.t, imm_of(r));
+    } else if (leaf(l) && e.op != PHCU_OP_POW) {  // ACC = B op ACC
+      gen(r, depth);
+      if (e.tb != T) emit(PHCU_I_CVT, 0, e.tb, 0, T);
+      emit(e.op, src_of(l), T, l.t, imm_of(l), 1);
+    } else {
+      if (depth >= 2) throw NotImplementedError("expression too deep for the two stash registers");
+      gen(r, depth);
+      emit(depth == 0 ? PHCU_I_ST0 : PHCU_I_ST1, 0, e.tb, 0, 0);
+      gen(l, depth + 1);
+      if (e.ta != T) emit(PHCU_I_CVT, 0, e.ta, 0, T);
+      emit(e.op, depth == 0 ? PHCU_SRC_S0 : PHCU_SRC_S1, T, e.tb, 0);
+    }
+    int32_t rt = T;
+    if (e.op == PHCU_OP_GT || e.op == PHCU_OP_LT || e.op == PHCU_OP_GE || e.op == PHCU_OP_LE || e.op == PHCU_OP_EQ)
+      rt = PHCU_BOOL;
+    else if (e.op == PHCU_OP_CMP)
+      rt = PHCU_I32;
+    else if (e.op == PHCU_OP_DIV && is_int_type(T))
+      rt = PHCU_F64;
+    if (rt != e.t) emit(PHCU_I_CVT, 0, rt, 0, e.t);
+  }
+};
+
+inline phcu_program_t compile_program(const ExprP& e, int32_t out_type, bool* raises) {
+  ProgramCompiler c;
+  c.run(e, out_type);
+  if (raises) *raises = c.raises;
+  return c.prog;
+}
+
+template <int32_t ID>
+struct TypeOf;
+template <>
+struct TypeOf<PHCU_F32> {
+  using type = float;
+};
+template <>
+struct TypeOf<PHCU_F64> {
+  using type = double;
+};
+template <>
+struct TypeOf<PHCU_I32> {
+  using type = int32_t;
+};
+template <>
+struct TypeOf<PHCU_I64> {
+  using type = int64_t;
+};
+}  // namespace detail
+
+// The element type of `a op b` for element types A and B, as Crystal types it.
+template <int32_t OP, typename A, typename B>
+using BinResult = typename detail::TypeOf<detail::result_type(OP, DType<A>::id, DType<B>::id)>::type;
+
+// The element handed to a process() block: operators on it record the
+// expression instead of computing, so the blocks of a chain compose into one
+// program (proc_view.cr:32-35).
+template <typename T>
+struct Sym {
+  using value_type = T;
+  detail::ExprP e;
+  // Operand `slot` of a program (for building expressions by hand).
+  static Sym input(int32_t slot) { return Sym{detail::input(slot, DType<T>::id)}; }
+};
+
+namespace detail {
+template <typename S>
+struct IsLiteral : std::false_type {};
+template <>
+struct IsLiteral<float> : std::true_type {};
+template <>
+struct IsLiteral<double> : std::true_type {};
+template <>
+struct IsLiteral<int32_t> : std::true_type {};
+template <>
+struct IsLiteral<int64_t> : std::true_type {};
+template <typename X>
+struct IsSym : std::false_type {};
+template <typename T>
+struct IsSym<Sym<T>> : std::true_type {};
+
+// One operand view of a fused expression: the buffer it keeps alive and its
+// layout.
+struct Leaf {
+  std::shared_ptr<Buffer> buf;
+  Affine aff;
+  int32_t dtype = 0;
+  phcu_view_t desc() const { return make_view(buf->ptr, dtype, aff); }
+  bool same(const Leaf& o) const {
+    return buf.get() == o.buf.get() && dtype == o.dtype && aff.offset == o.aff.offset && aff.shape == o.aff.shape &&
+           aff.stride == o.aff.stride;
+  }
+};
+
+inline std::string shape_text(const std::vector<int64_t>& s) {
+  std::string t = "[";
+  for (size_t i = 0; i < s.size(); i++) t += (i ? ", " : "") + std::to_string(s[i]);
+  return t + "]";
+}
+
+inline const char* op_name(int32_t op) {
+  static const char* names[] = {"+", "-", "*", "/", "//", "%", "**", "&+", "&-", "&*", "&**", "&", "|", "^"};
+  return op >= 0 && op < (int32_t)(sizeof(names) / sizeof(names[0])) ? names[op] : "?";
+}
+}  // namespace detail
+
+// A lazy elementwise program over up to PHCU_MAX_INPUTS aliasing operand views
+// (ProcView, src/proc_view.cr:6-35).  process() composes blocks; infix
+// operators with other fused expressions, views, arrays or constants extend
+// the program; the whole chain runs as ONE kernel when it is materialised
+// (to_cu / to_vector / get_chunk / a reduction / set_chunk).  Identical
+// operand views share one input slot.
+template <typename T>
+class CuProcView {
+ public:
+  CuProcView(std::vector<detail::Leaf> leaves, detail::ExprP expr, std::vector<int64_t> shape)
+      : leaves_(std::move(leaves)), expr_(std::move(expr)), shape_(std::move(shape)) {
+    std::vector<detail::Leaf> kept;
+    std::vector<int32_t> slot(leaves_.size());
+    for (size_t i = 0; i < leaves_.size(); i++) {
+      size_t j = 0;
+      while (j < kept.size() && !kept[j].same(leaves_[i])) j++;
+      if (j == kept.size()) kept.push_back(leaves_[i]);
+      slot[i] = (int32_t)j;
+    }
+    if (kept.size() != leaves_.size()) {
+      expr_ = detail::relabel(expr_, [&slot](int32_t k) { return slot[k]; });
+      leaves_ = std::move(kept);
+    }
+  }
+
+  const std::vector<int64_t>& shape() const { return shape_; }
+  int64_t size() const { return shape_to_size(shape_); }
+  size_t dimensions() const { return shape_.size(); }
+  const std::vector<detail::Leaf>& leaves() const { return leaves_; }
+  const detail::ExprP& expr() const { return expr_; }
+
+  // ProcView#process (proc_view.cr:32-35): another block on the result.
+  template <typename F>
+  auto process(F f) const {
+    auto r = f(Sym<T>{expr_});
+    using R = decltype(r);
+    if constexpr (detail::IsLiteral<R>::value) {
+      return CuProcView<R>(leaves_, detail::constant(r), shape_);  // a constant block
+    } else {
+      static_assert(detail::IsSym<R>::value, "a process block returns a Sym or a constant");
+      return CuProcView<typename R::value_type>(leaves_, r.e, shape_);
+    }
+  }
+
+  // Index transforms commute with an elementwise program, so view / permute /
+  // reverse apply to every operand and the program stays as it is.
+  CuProcView view(const std::vector<Lit>& region) const {
+    const IndexRegion r = IndexRegion::make(region, shape_);
+    std::vector<detail::Leaf> ls = leaves_;
+    for (auto& l : ls) l.aff = affine_region(l.aff, r);
+    return CuProcView(std::move(ls), expr_, affine_region(Affine{0, shape_, row_major(shape_)}, r).shape);
+  }
+  CuProcView permute(std::vector<int> order = {}) const {
+    if (order.empty())
+      for (size_t i = shape_.size(); i-- > 0;) order.push_back((int)i);
+    std::vector<detail::Leaf> ls = leaves_;
+    for (auto& l : ls) l.aff = affine_permute(l.aff, order);
+    return CuProcView(std::move(ls), expr_, affine_permute(Affine{0, shape_, row_major(shape_)}, order).shape);
+  }
+  CuProcView reverse() const {
+    std::vector<detail::Leaf> ls = leaves_;
+    for (auto& l : ls) l.aff = affine_reverse(l.aff);
+    return CuProcView(std::move(ls), expr_, shape_);
+  }
+
+  // The device program this expression compiles to; `raises` tells whether
+  // it can set the status word (checked Int arithmetic).
+  phcu_program_t program(bool* raises = nullptr) const {
+    return detail::compile_program(expr_, DType<T>::id, raises);
+  }
+
+  // One phcu_eval into a new contiguous array.
+  CuNArray<T> to_cu() const {
+    if (leaves_.size() > (size_t)PHCU_MAX_INPUTS)
+      throw NotImplementedError("a fused program reads at most " + std::to_string(PHCU_MAX_INPUTS) +
+                                " distinct views");
+    bool raises = false;
+    const phcu_program_t p = program(&raises);
+    CuNArray<T> out(shape_);
+    phcu_view_t ins[PHCU_MAX_INPUTS];
+    std::memset(ins, 0, sizeof(ins));
+    for (size_t k = 0; k < leaves_.size(); k++) ins[k] = leaves_[k].desc();
+    const phcu_view_t o = out.desc();
+    check(phcu_eval(&p, ins, (int32_t)leaves_.size(), &o), "phcu_eval");
+    if (raises) check_status();
+    return out;
+  }
+  std::vector<T> to_vector() const { return to_cu().to_vector(); }
+  // MultiIndexable#get_chunk: evaluates the region's elements only.
+  CuNArray<T> get_chunk(const std::vector<Lit>& region) const { return view(region).to_cu(); }
+
+ private:
+  std::vector<detail::Leaf> leaves_;
+  detail::ExprP expr_;
+  std::vector<int64_t> shape_;
+};
+
+template <typename T>
+CuProcView<T> CuView<T>::process() const {
+  return CuProcView<T>({detail::Leaf{buf_, aff_, DType<T>::id}}, detail::input(0, DType<T>::id), aff_.shape);
+}
+
+template <typename T>
+template <typename F>
+auto CuView<T>::process(F f) const {
+  return process().process(f);
+}
+
+namespace detail {
+template <typename T>
+CuProcView<T> lift(const CuView<T>& v) {
+  return v.process();
+}
+
+template <int32_t OP, typename A, typename B>
+CuProcView<BinResult<OP, A, B>> combine(const CuProcView<A>& a, const CuProcView<B>& b) {
+  if (a.shape() != b.shape())
+    throw ShapeError("The shape of this MultiIndexable (" + shape_text(a.shape()) +
+                     ") does not match the shape of the one provided (" + shape_text(b.shape()) + "), so '" +
+                     op_name(OP) + "' cannot be applied element-wise.");
+  std::vector<Leaf> leaves = a.leaves();
+  const int32_t base = (int32_t)leaves.size();
+  leaves.insert(leaves.end(), b.leaves().begin(), b.leaves().end());
+  ExprP rhs = relabel(b.expr(), [base](int32_t k) { return k + base; });
+  return CuProcView<BinResult<OP, A, B>>(std::move(leaves), binary_expr(OP, a.expr(), rhs), a.shape());
+}
+}  // namespace detail
+
+// The lazy operators: on two Syms or a Sym and a constant (inside process
+// blocks), and on a fused expression with another one, a view / array or a
+// constant.  Constants take Crystal's literal types: int -> Int32, long
+// (int64_t) -> Int64, float -> Float32, double -> Float64.  Eager operators
+// between two plain views stay as they are (one kernel each).
+#define PHASE_LAZY_BINARY(NAME, OPCODE)                                                                       \
+  template <typename A, typename B>                                                                           \
+  Sym<BinResult<OPCODE, A, B>> NAME(const Sym<A>& a, const Sym<B>& b) {                                       \
+    return {detail::binary_expr(OPCODE, a.e, b.e)};                                                           \
+  }                                                                                                           \
+  template <typename A, typename S, typename = std::enable_if_t<detail::IsLiteral<S>::value>>                 \
+  Sym<BinResult<OPCODE, A, S>> NAME(const Sym<A>& a, S s) {                                                   \
+    return {detail::binary_expr(OPCODE, a.e, detail::constant(s))};                                           \
+  }                                                                                                           \
+  template <typename S, typename B, typename = std::enable_if_t<detail::IsLiteral<S>::value>>                 \
+  Sym<BinResult<OPCODE, S, B>> NAME(S s, const Sym<B>& b) {                                                   \
+    return {detail::binary_expr(OPCODE, detail::constant(s), b.e)};                                           \
+  }                                                                                                           \
+  template <typename A, typename B>                                                                           \
+  CuProcView<BinResult<OPCODE, A, B>> NAME(const CuProcView<A>& a, const CuProcView<B>& b) {                  \
+    return detail::combine<OPCODE>(a, b);                                                                     \
+  }                                                                                                           \
+  template <typename A, typename B>                                                                           \
+  CuProcView<BinResult<OPCODE, A, B>> NAME(const CuProcView<A>& a, const CuView<B>& b) {                      \
+    return detail::combine<OPCODE>(a, detail::lift(b));                                                       \
+  }                                                                                                           \
+  template <typename A, typename B>                                                                           \
+  CuProcView<BinResult<OPCODE, A, B>> NAME(const CuView<A>& a, const CuProcView<B>& b) {                      \
+    return detail::combine<OPCODE>(detail::lift(a), b);                                                       \
+  }                                                                                                           \
+  template <typename A, typename S, typename = std::enable_if_t<detail::IsLiteral<S>::value>>                 \
+  CuProcView<BinResult<OPCODE, A, S>> NAME(const CuProcView<A>& a, S s) {                                     \
+    return CuProcView<BinResult<OPCODE, A, S>>(a.leaves(), detail::binary_expr(OPCODE, a.expr(),              \
+                                                                               detail::constant(s)),          \
+                                               a.shape());                                                    \
+  }                                                                                                           \
+  template <typename S, typename B, typename = std::enable_if_t<detail::IsLiteral<S>::value>>                 \
+  CuProcView<BinResult<OPCODE, S, B>> NAME(S s, const CuProcView<B>& b) {                                     \
+    return CuProcView<BinResult<OPCODE, S, B>>(b.leaves(), detail::binary_expr(OPCODE, detail::constant(s),   \
+                                                                               b.expr()),                     \
+                                               b.shape());                                                    \
+  }
+
+PHASE_LAZY_BINARY(operator+, PHCU_OP_ADD)
+PHASE_LAZY_BINARY(operator-, PHCU_OP_SUB)
+PHASE_LAZY_BINARY(operator*, PHCU_OP_MUL)
+PHASE_LAZY_BINARY(operator/, PHCU_OP_DIV)
+PHASE_LAZY_BINARY(operator%, PHCU_OP_MOD)
+PHASE_LAZY_BINARY(operator&, PHCU_OP_AND)
+PHASE_LAZY_BINARY(operator|, PHCU_OP_OR)
+PHASE_LAZY_BINARY(operator^, PHCU_OP_XOR)
+PHASE_LAZY_BINARY(floordiv, PHCU_OP_FLOORDIV)  // Crystal //
+PHASE_LAZY_BINARY(pow, PHCU_OP_POW)            // Crystal **
+PHASE_LAZY_BINARY(wadd, PHCU_OP_WADD)          // Crystal &+
+PHASE_LAZY_BINARY(wsub, PHCU_OP_WSUB)          // Crystal &-
+PHASE_LAZY_BINARY(wmul, PHCU_OP_WMUL)          // Crystal &*
+PHASE_LAZY_BINARY(wpow, PHCU_OP_WPOW)          // Crystal &**
+#undef PHASE_LAZY_BINARY
+
+// Unary minus (multi_indexable.cr:983-985); checked for Int operands.
+template <typename T>
+Sym<T> operator-(const Sym<T>& a) {
+  return {detail::unary_expr(PHCU_I_NEG, a.e)};
+}
+template <typename T>
+CuProcView<T> operator-(const CuProcView<T>& a) {
+  return CuProcView<T>(a.leaves(), detail::unary_expr(PHCU_I_NEG, a.expr()), a.shape());
+}
+
 // ------------------------------------------------------------ reductions
 // Enumerable#sum / #max / #min over the slices along an axis (multi_indexable.cr:
 // 18, 742-786) and the argmax idiom (README.md:56-61: the first maximum wins).
@@ -727,5 +1221,29 @@ std::vector<int64_t> argmin(const CuView<T>& a) {
   if (a.size() == 0) throw EmptyError("Empty enumerable");
   return detail::unravel(detail::reduce_all<int64_t>(PHCU_RED_ARGMIN, a), a.shape());
 }
+
+
+// Reductions of a fused expression: the program runs once into a temporary,
+// then the reduction kernel reads it.
+template <typename T>
+CuNArray<T> sum(const CuProcView<T>& a, int axis) { return sum(a.to_cu(), axis); }
+template <typename T>
+CuNArray<T> max(const CuProcView<T>& a, int axis) { return max(a.to_cu(), axis); }
+template <typename T>
+CuNArray<T> min(const CuProcView<T>& a, int axis) { return min(a.to_cu(), axis); }
+template <typename T>
+CuNArray<int32_t> argmax(const CuProcView<T>& a, int axis) { return argmax(a.to_cu(), axis); }
+template <typename T>
+CuNArray<int32_t> argmin(const CuProcView<T>& a, int axis) { return argmin(a.to_cu(), axis); }
+template <typename T>
+T sum(const CuProcView<T>& a) { return sum(a.to_cu()); }
+template <typename T>
+T max(const CuProcView<T>& a) { return max(a.to_cu()); }
+template <typename T>
+T min(const CuProcView<T>& a) { return min(a.to_cu()); }
+template <typename T>
+std::vector<int64_t> argmax(const CuProcView<T>& a) { return argmax(a.to_cu()); }
+template <typename T>
+std::vector<int64_t> argmin(const CuProcView<T>& a) { return argmin(a.to_cu()); }
 
 }  // namespace phase

@@ -2,7 +2,8 @@
 // reads a.f32/b.f32/a.i32/b.i32 (16x12x10, row-major) from the directory
 // given as argv[1], writes each result as <name>.bin there and prints one line
 // per result or raised exception; tests/test_gpu_host_cpp.py compares them
-// with the oracle.
+// with the oracle.  With argv[2] = "proc" it runs the fused expressions
+// (CuProcView) instead of the eager operators.
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -43,6 +44,8 @@ static void expect_raise(const std::string& name, F f) {
     std::cout << "raised " << name << " IndexError\n";
   } catch (const OverflowError&) {
     std::cout << "raised " << name << " OverflowError\n";
+  } catch (const NotImplementedError&) {
+    std::cout << "raised " << name << " NotImplementedError\n";
   }
 }
 
@@ -80,9 +83,61 @@ static void run(const std::string& tag) {
   expect_raise(tag + "_dim", [&] { return A.view({all(), all(), all(), all()}); });
 }
 
+// Fused chains: one phcu_eval per materialisation.
+template <typename T>
+static void run_proc(const std::string& tag) {
+  const std::vector<int64_t> shape = {16, 12, 10};
+  const size_t n = 16 * 12 * 10;
+  const CuNArray<T> A = CuNArray<T>::of_buffer(shape, load<T>("a." + tag, n));
+  const CuNArray<T> B = CuNArray<T>::of_buffer(shape, load<T>("b." + tag, n));
+  const std::vector<Lit> rev = {all(), rng(std::nullopt, std::nullopt, -1), all()};
+  // ((x + 4) ** 2) * y - z over an array and two reversed views
+  const auto chain = A.process([](auto e) { return pow(e + 4, 2); }) * B.view(rev) - A.view(rev);
+  save(tag + "_proc_chain", chain.to_vector());
+  save(tag + "_proc_chain_perm", chain.permute({2, 0, 1}).reverse().to_vector());
+  save(tag + "_proc_chain_max1", max(chain, 1).to_vector());
+  save(tag + "_proc_chain_argmax0", argmax(chain, 0).to_vector());
+  save(tag + "_proc_sum1", sum(A.process() * 3 - B.view(rev), 1).to_vector());  // within Int32
+  save(tag + "_proc_chain_chunk", chain.get_chunk({idx(3), rng(0, 10, 3, true)}).to_vector());
+  CuNArray<T> C = CuNArray<T>::fill(shape, T(0));
+  C.set_chunk(rev, A.process() + B);
+  save(tag + "_proc_set", C.to_vector());
+  CuNArray<T> D = A.clone();
+  D.set_chunk({rng(1, -1)}, D.view({rng(0, -2)}).process() * 2);  // reads the rows it writes
+  save(tag + "_proc_overlap", D.to_vector());
+  save(tag + "_proc_const", A.process([](auto) { return 2.5f; }).to_vector());
+  expect_raise(tag + "_proc_five",
+               [&] { return ((A.process() + B) * (A.view(rev) - B.view(rev)) + A.reverse()).to_cu(); });
+}
+
+static void run_proc_mixed() {
+  const std::vector<int64_t> shape = {16, 12, 10};
+  const size_t n = 16 * 12 * 10;
+  const CuNArray<float> A = CuNArray<float>::of_buffer(shape, load<float>("a.f32", n));
+  const CuNArray<int32_t> Ai = CuNArray<int32_t>::of_buffer(shape, load<int32_t>("a.i32", n));
+  const CuNArray<int32_t> Bi = CuNArray<int32_t>::of_buffer(shape, load<int32_t>("b.i32", n));
+  save("proc_mixed", ((Ai.process() * 0.5f + A) / 3.0).to_vector());      // Int32 * Float32, then Float64
+  save("proc_div", (Ai.permute({2, 0, 1}).process() / Bi.permute({2, 0, 1})).to_vector());  // Float64
+  const CuNArray<int32_t> big = CuNArray<int32_t>::fill({64}, 1 << 30);
+  expect_raise("proc_overflow", [&] { return (big.process() * 4 + big).to_cu(); });
+  save("proc_wrapped", wadd(wmul(big.process(), 4), big).to_vector());
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
   dir = argv[1];
+  if (argc > 2 && std::string(argv[2]) == "proc") {
+    try {
+      init(0);
+      run_proc<float>("f32");
+      run_proc<int32_t>("i32");
+      run_proc_mixed();
+    } catch (const std::exception& e) {
+      std::cout << "error " << e.what() << "\n";
+      return 1;
+    }
+    return 0;
+  }
   try {
     init(0);
     run<float>("f32");

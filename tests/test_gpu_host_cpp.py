@@ -1,8 +1,8 @@
 """The C++ host mirror (ph-core_gb300/host/phase.hpp) on the device: views,
-infix operators with Crystal's result types, reductions, chunk reads and
-writes and the reference's exceptions, checked against the oracle on
-16x12x10 Float32 and Int32 arrays (bit-exact; sums within 1e-6 relative of
-the FP64 oracle)."""
+infix operators with Crystal's result types, fused chains (CuProcView: one
+program per materialisation), reductions, chunk reads and writes and the
+reference's exceptions, checked against the oracle on 16x12x10 Float32 and
+Int32 arrays (bit-exact; sums within 1e-6 relative of the FP64 oracle)."""
 import os
 import shutil
 import subprocess
@@ -29,7 +29,8 @@ def _cuda_lib_dir():
 
 
 @pytest.fixture(scope="module")
-def run(tmp_path_factory, cu):
+def built(tmp_path_factory, cu):
+    """(driver executable, work directory, input arrays)."""
     from phase_cu import synth
 
     gxx = shutil.which("g++")
@@ -52,7 +53,12 @@ def run(tmp_path_factory, cu):
     for tag, (a, b) in arrays.items():
         a.tofile(str(d / ("a." + tag)))
         b.tofile(str(d / ("b." + tag)))
-    p = subprocess.run([exe, str(d)], capture_output=True, text=True, timeout=300)
+    return exe, d, arrays
+
+
+def _drive(built, *mode):
+    exe, d, arrays = built
+    p = subprocess.run([exe, str(d)] + list(mode), capture_output=True, text=True, timeout=300)
     assert p.returncode == 0, p.stdout[-2000:] + p.stderr[-2000:]
     lines = p.stdout.splitlines()
 
@@ -60,6 +66,16 @@ def run(tmp_path_factory, cu):
         return np.fromfile(str(d / (name + ".bin")), dtype=dtype)
 
     return arrays, lines, load
+
+
+@pytest.fixture(scope="module")
+def run(built):
+    return _drive(built)
+
+
+@pytest.fixture(scope="module")
+def run_proc(built):
+    return _drive(built, "proc")
 
 
 @pytest.mark.parametrize("tag", ["f32", "i32"])
@@ -127,3 +143,61 @@ def test_checked_and_wrapping_int32(run):
     _, lines, load = run
     assert "raised overflow OverflowError" in lines
     assert np.all(load("wrapped", np.int32) == np.int32(-2 ** 31))
+
+
+@pytest.mark.parametrize("tag", ["f32", "i32"])
+def test_fused_chains(run_proc, ora, tag):
+    """CuProcView: ((x + 4) ** 2) * y - z as one program, checked against the
+    reference's one pass per operator; its permuted / reversed / chunked
+    forms, reductions and writes."""
+    arrays, lines, load = run_proc
+    a, b = arrays[tag]
+    dt = a.dtype
+    t = ora.I32
+    rev = lambda x: np.ascontiguousarray(x[:, ::-1, :])  # noqa: E731
+    chain, _ = ora.map_binary_scalar(ora.OP_ADD, a, 4, t)
+    chain, _ = ora.map_binary_scalar(ora.OP_POW, chain, 2, t)
+    chain, _ = ora.map_binary(ora.OP_MUL, chain, rev(b))
+    chain, _ = ora.map_binary(ora.OP_SUB, chain, rev(a))
+    assert chain.dtype == dt
+    assert np.array_equal(load(tag + "_proc_chain", dt), chain.reshape(-1))
+    perm = np.transpose(chain, (2, 0, 1))[::-1, ::-1, ::-1]
+    assert np.array_equal(load(tag + "_proc_chain_perm", dt), perm.reshape(-1))
+    assert np.array_equal(load(tag + "_proc_chain_chunk", dt), chain[3, 0:10:3, :].reshape(-1))
+    assert np.array_equal(load(tag + "_proc_chain_max1", dt), ora.reduce(ora.RED_MAX, chain, 1).reshape(-1))
+    assert np.array_equal(load(tag + "_proc_chain_argmax0", np.int32),
+                          ora.reduce(ora.RED_ARGMAX, chain, 0, ora.I32).reshape(-1))
+    lin, _ = ora.map_binary_scalar(ora.OP_MUL, a, 3, t)
+    lin, _ = ora.map_binary(ora.OP_SUB, lin, rev(b))
+    s1 = load(tag + "_proc_sum1", dt)
+    if tag == "f32":
+        ref = ora.reduce_f64(lin, 1).reshape(-1)
+        mag = ora.reduce_f64(np.abs(lin), 1).reshape(-1)
+        assert np.all(np.abs(s1 - ref) <= 1e-6 * mag + 1e-30)  # tolerance: 1e-6 of the sum of magnitudes
+    else:
+        assert np.array_equal(s1, ora.reduce(ora.RED_SUM, lin, 1).reshape(-1))
+    c = np.zeros_like(a)
+    c[:, ::-1, :] = ora.map_binary(ora.OP_ADD, a, b)[0]
+    assert np.array_equal(load(tag + "_proc_set", dt), c.reshape(-1))
+    d = a.copy()
+    d[1:] = ora.map_binary_scalar(ora.OP_MUL, np.ascontiguousarray(a[:-1]), 2, t)[0]
+    assert np.array_equal(load(tag + "_proc_overlap", dt), d.reshape(-1))
+    assert np.all(load(tag + "_proc_const", np.float32) == np.float32(2.5))
+    assert "raised %s_proc_five NotImplementedError" % tag in lines  # five operand views
+
+
+def test_fused_mixed_types_and_checked_int32(run_proc, ora):
+    arrays, lines, load = run_proc
+    a, _ = arrays["f32"]
+    ai, bi = arrays["i32"]
+    m, _ = ora.map_binary_scalar(ora.OP_MUL, ai, 0.5, ora.F32)  # Int32 * Float32 -> Float32
+    m, _ = ora.map_binary(ora.OP_ADD, m, a)
+    m, _ = ora.map_binary_scalar(ora.OP_DIV, m, 3.0, ora.F64)  # Float32 / Float64 -> Float64
+    assert m.dtype == np.float64
+    assert np.array_equal(load("proc_mixed", np.float64), m.reshape(-1))
+    ap = np.ascontiguousarray(np.transpose(ai, (2, 0, 1)))
+    bp = np.ascontiguousarray(np.transpose(bi, (2, 0, 1)))
+    q, _ = ora.map_binary(ora.OP_DIV, ap, bp)  # Int32 / Int32 -> Float64, zero divisors give Inf / NaN
+    assert np.array_equal(load("proc_div", np.float64), q.reshape(-1), equal_nan=True)
+    assert "raised proc_overflow OverflowError" in lines
+    assert np.all(load("proc_wrapped", np.int32) == np.int32(2 ** 30))
