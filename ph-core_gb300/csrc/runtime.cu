@@ -93,16 +93,26 @@ int blocks_per_sm(const void* fn, int threads, size_t smem) {
   return per_sm;
 }
 
-}  // namespace phcu
+// Frees what a context holds (any subset of it, after a failed init) and
+// resets it.
+static void release_context(Context& c) {
+  if (c.stream && c.stream != c.own_stream) cudaStreamSynchronize(c.stream);  // a caller's stream
+  if (c.own_stream) cudaStreamSynchronize(c.own_stream);
+  if (c.d2h) cudaStreamSynchronize(c.d2h);
+  if (c.h2d) cudaStreamSynchronize(c.h2d);
+  if (c.l2_scrub) cudaFree(c.l2_scrub);
+  if (c.status) cudaFree(c.status);
+  if (c.ev_work) cudaEventDestroy(c.ev_work);
+  if (c.ev_h2d) cudaEventDestroy(c.ev_h2d);
+  if (c.d2h) cudaStreamDestroy(c.d2h);
+  if (c.h2d) cudaStreamDestroy(c.h2d);
+  if (c.own_stream) cudaStreamDestroy(c.own_stream);
+  c = Context();
+  g_nocc = 0;  // attributes and occupancy belong to this device's context
+  g_nlim = 0;
+}
 
-using namespace phcu;
-
-extern "C" {
-
-int32_t phcu_init(int32_t device) {
-  Context& c = g_ctx;
-  if (c.ready && c.device == device) return PHCU_OK;
-  if (c.ready) return fail(PHCU_ERR_INVALID, "phcu_init: already initialised on device %d", c.device);
+static int32_t create_context(Context& c, int32_t device) {
   PHCU_CUDA(cudaSetDevice(device));
   PHCU_CUDA(cudaStreamCreateWithFlags(&c.own_stream, cudaStreamNonBlocking));
   c.stream = c.own_stream;
@@ -132,22 +142,28 @@ int32_t phcu_init(int32_t device) {
   return PHCU_OK;
 }
 
-int32_t phcu_shutdown(void) {
+}  // namespace phcu
+
+using namespace phcu;
+
+extern "C" {
+
+int32_t phcu_init(int32_t device) {
   Context& c = g_ctx;
-  if (!c.ready) return PHCU_OK;
-  cudaStreamSynchronize(c.stream);
-  cudaStreamSynchronize(c.d2h);
-  cudaStreamSynchronize(c.h2d);
-  if (c.l2_scrub) cudaFree(c.l2_scrub);
-  cudaFree(c.status);
-  cudaEventDestroy(c.ev_work);
-  cudaEventDestroy(c.ev_h2d);
-  cudaStreamDestroy(c.d2h);
-  cudaStreamDestroy(c.h2d);
-  cudaStreamDestroy(c.own_stream);
-  c = Context();
-  g_nocc = 0;  // attributes and occupancy belong to this device's context
-  g_nlim = 0;
+  if (c.ready && c.device == device) return PHCU_OK;
+  if (c.ready) return fail(PHCU_ERR_INVALID, "phcu_init: already initialised on device %d", c.device);
+  const int32_t rc = create_context(c, device);
+  if (rc != PHCU_OK) {
+    char msg[512];
+    phcu_last_error(msg, sizeof(msg));
+    release_context(c);  // a failed init leaves nothing behind; phcu_init may be called again
+    return fail(rc, "%s", msg);
+  }
+  return PHCU_OK;
+}
+
+int32_t phcu_shutdown(void) {
+  if (g_ctx.ready) release_context(g_ctx);
   return PHCU_OK;
 }
 
@@ -224,6 +240,7 @@ int32_t phcu_free(void* dptr) {
 
 int32_t phcu_host_alloc(size_t bytes, void** hptr) {
   PHCU_TRY(require_ctx());
+  if (!hptr) return fail(PHCU_ERR_INVALID, "phcu_host_alloc: null output pointer");
   PHCU_CUDA(cudaMallocHost(hptr, bytes ? bytes : 16));
   return PHCU_OK;
 }
@@ -320,25 +337,37 @@ int32_t phcu_graph_destroy(void* graph_exec) {
   return PHCU_OK;
 }
 
+static void timer_release(Timer* t) {
+  if (t->a) cudaEventDestroy(t->a);
+  if (t->b) cudaEventDestroy(t->b);
+  delete t;
+}
+
 int32_t phcu_timer_start(void** timer) {
   PHCU_TRY(require_ctx());
-  Timer* t = new Timer();
-  PHCU_CUDA(cudaEventCreate(&t->a));
-  PHCU_CUDA(cudaEventCreate(&t->b));
-  PHCU_CUDA(cudaEventRecord(t->a, g_ctx.stream));
+  if (!timer) return fail(PHCU_ERR_INVALID, "phcu_timer_start: null output pointer");
+  Timer* t = new Timer{nullptr, nullptr};
+  cudaError_t e = cudaEventCreate(&t->a);
+  if (e == cudaSuccess) e = cudaEventCreate(&t->b);
+  if (e == cudaSuccess) e = cudaEventRecord(t->a, g_ctx.stream);
+  if (e != cudaSuccess) {
+    timer_release(t);
+    return cuda_fail(e, "phcu_timer_start");
+  }
   *timer = t;
   return PHCU_OK;
 }
 
+// Stops and releases the timer, whether or not the measurement succeeds.
 int32_t phcu_timer_stop(void* timer, float* ms) {
   PHCU_TRY(require_ctx());
+  if (!timer || !ms) return fail(PHCU_ERR_INVALID, "phcu_timer_stop: null pointer");
   Timer* t = (Timer*)timer;
-  PHCU_CUDA(cudaEventRecord(t->b, g_ctx.stream));
-  PHCU_CUDA(cudaEventSynchronize(t->b));
-  PHCU_CUDA(cudaEventElapsedTime(ms, t->a, t->b));
-  cudaEventDestroy(t->a);
-  cudaEventDestroy(t->b);
-  delete t;
+  cudaError_t e = cudaEventRecord(t->b, g_ctx.stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(t->b);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(ms, t->a, t->b);
+  timer_release(t);
+  if (e != cudaSuccess) return cuda_fail(e, "phcu_timer_stop");
   return PHCU_OK;
 }
 
