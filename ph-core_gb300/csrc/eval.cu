@@ -142,27 +142,32 @@ static int32_t check_program(const phcu_program_t* prog, int nin) {
 }
 
 // Evaluates with inputs that may overlap the output: an input that overlaps
-// the output with a different mapping is first copied to a temporary.
+// the output with a different mapping is first copied to a temporary.  Every
+// argument is checked before the context is asked for, so argument errors
+// come back the same with or without a device.
 int32_t eval_views(const phcu_program_t* prog, const phcu_view_t* inputs, int nin, const phcu_view_t* out,
                    int force_mode = -1) {
-  PHCU_TRY(require_ctx());
   PHCU_TRY(check_view(out, "output"));
   if (nin < 0 || nin > MAXIN) return fail(PHCU_ERR_INVALID, "n_inputs %d outside 0..%d", nin, MAXIN);
+  if (nin > 0 && !inputs) return fail(PHCU_ERR_INVALID, "null input array");
   for (int k = 0; k < nin; k++) PHCU_TRY(check_view(&inputs[k], "input"));
   PHCU_TRY(check_program(prog, nin));
   if (prog->out_type != out->dtype)
     return fail(PHCU_ERR_INVALID, "program result type %d differs from output dtype %d", prog->out_type, out->dtype);
+  PHCU_TRY(require_ctx());
 
   phcu_view_t staged[MAXIN];
   void* temps[MAXIN] = {nullptr};
   const phcu_view_t* ins[MAXIN];
-  for (int k = 0; k < nin; k++) {
-    ins[k] = &inputs[k];
+  int32_t rc = PHCU_OK;
+  for (int k = 0; k < nin; k++) ins[k] = &inputs[k];
+  for (int k = 0; k < nin && rc == PHCU_OK; k++) {
     if (views_overlap(&inputs[k], out) && !views_identical(&inputs[k], out)) {
       // materialise this input first (lexicographic, contiguous)
       const phcu_view_t& v = inputs[k];
       int64_t n = view_size(&v);
-      PHCU_TRY(scratch_alloc((size_t)n * dtype_size(v.dtype), &temps[k]));
+      rc = scratch_alloc((size_t)n * dtype_size(v.dtype), &temps[k]);
+      if (rc != PHCU_OK) break;
       phcu_view_t t;
       memset(&t, 0, sizeof(t));
       t.base = temps[k];
@@ -184,22 +189,24 @@ int32_t eval_views(const phcu_program_t* prog, const phcu_view_t* inputs, int ni
       cp.code[0].type = (uint8_t)v.dtype;
       cp.code[0].btype = (uint8_t)v.dtype;
       const phcu_view_t* one[1] = {&v};
-      PHCU_TRY(make_plan(&t, one, 1, &C.plan));
+      rc = make_plan(&t, one, 1, &C.plan);
       C.prog = cp;
       C.status = ctx().status;
-      if (C.plan.mode != MODE_EMPTY) PHCU_TRY(launch_eval(C));
+      if (rc == PHCU_OK && C.plan.mode != MODE_EMPTY) rc = launch_eval(C);
       staged[k] = t;
       ins[k] = &staged[k];
     }
   }
-  EvalArgs A;
-  int32_t rc = make_plan(out, ins, nin, &A.plan, force_mode);
-  if (rc == PHCU_OK && A.plan.mode != MODE_EMPTY) {
-    A.prog = *prog;
-    A.status = ctx().status;
-    rc = launch_eval(A);
+  if (rc == PHCU_OK) {
+    EvalArgs A;
+    rc = make_plan(out, ins, nin, &A.plan, force_mode);
+    if (rc == PHCU_OK && A.plan.mode != MODE_EMPTY) {
+      A.prog = *prog;
+      A.status = ctx().status;
+      rc = launch_eval(A);
+    }
   }
-  for (int k = 0; k < nin; k++) scratch_free(temps[k]);
+  for (int k = 0; k < nin; k++) scratch_free(temps[k]);  // stream-ordered after the launches
   return rc;
 }
 
@@ -330,7 +337,6 @@ int32_t phcu_result_dtype(int32_t op, int32_t ta, int32_t tb, int32_t* tout) {
 }
 
 int32_t phcu_copy(const phcu_view_t* dst, const phcu_view_t* src) {
-  PHCU_TRY(require_ctx());
   PHCU_TRY(check_view(dst, "dst"));
   PHCU_TRY(check_view(src, "src"));
   if (dst->dtype != src->dtype)
@@ -350,7 +356,6 @@ int32_t phcu_copy(const phcu_view_t* dst, const phcu_view_t* src) {
 }
 
 int32_t phcu_fill(const phcu_view_t* dst, const phcu_scalar_t* value) {
-  PHCU_TRY(require_ctx());
   PHCU_TRY(check_view(dst, "dst"));
   if (!value) return fail(PHCU_ERR_INVALID, "phcu_fill: null value");
   phcu_program_t P;

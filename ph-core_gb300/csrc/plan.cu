@@ -29,12 +29,22 @@ int32_t check_view(const phcu_view_t* v, const char* what) {
   if (!v) return fail(PHCU_ERR_INVALID, "%s: null view", what);
   if (!dtype_valid(v->dtype)) return fail(PHCU_ERR_INVALID, "%s: bad dtype %d", what, v->dtype);
   if (v->rank < 0 || v->rank > MAXR) return fail(PHCU_ERR_DIM, "%s: rank %d outside 0..%d", what, v->rank, MAXR);
-  for (int i = 0; i < v->rank; i++)
+  bool empty = false;
+  for (int i = 0; i < v->rank; i++) {
     if (v->shape[i] < 0) return fail(PHCU_ERR_DIM, "%s: negative extent on axis %d", what, i);
-  if (view_size(v) > 0 && !v->base) return fail(PHCU_ERR_INVALID, "%s: null base pointer", what);
-  if (view_size(v) >= (int64_t)UINT32_MAX)
-    return fail(PHCU_ERR_UNSUPPORTED, "%s: %lld elements exceed the 2^32-1 per-operation limit", what,
-                (long long)view_size(v));
+    if (v->shape[i] == 0) empty = true;
+  }
+  if (empty) return PHCU_OK;
+  // the element count, refused before the product could wrap: n * s stays
+  // within the limit exactly when n <= limit / s (integer division)
+  const int64_t limit = (int64_t)UINT32_MAX - 1;
+  int64_t n = 1;
+  for (int i = 0; i < v->rank; i++) {
+    if (n > limit / v->shape[i])
+      return fail(PHCU_ERR_UNSUPPORTED, "%s: more than 2^32-2 elements (the per-operation limit)", what);
+    n *= v->shape[i];
+  }
+  if (!v->base) return fail(PHCU_ERR_INVALID, "%s: null base pointer", what);
   return PHCU_OK;
 }
 

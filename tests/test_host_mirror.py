@@ -301,6 +301,57 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
 
 
+def test_views_are_checked_before_the_device():
+    """phcu_copy / phcu_fill / phcu_eval check views, the input array and the
+    program on the host before they ask for a context, so these calls run
+    here without a GPU.  Element counts are refused before their product can
+    wrap: [3, 6148914691236517206] holds 2^64 + 2 elements, which a wrapped
+    count would take for 2."""
+    import __graft_entry__
+    from phase_cu import _abi as A
+
+    if not os.path.exists(os.path.join(ROOT, "ph-core_gb300", "phase_cu", "_lib", "libphcuda.so")):
+        __graft_entry__.build()
+    lib = A.load()
+
+    def view(shape, base=0x1000):
+        v = A.View()
+        v.base, v.dtype, v.rank = base, A.F32, len(shape)
+        for i, s in enumerate(shape):
+            v.shape[i], v.stride[i] = s, 1
+        return v
+
+    def copy(shape, base=0x1000):
+        d, s = view(shape, base), view(shape, base)
+        return lib.phcu_copy(ctypes.byref(d), ctypes.byref(s))
+
+    limit = 2 ** 32 - 2  # elements per operation
+    assert copy([3, 6148914691236517206]) == A.ERR_UNSUPPORTED
+    assert copy([2 ** 31, 2]) == A.ERR_UNSUPPORTED
+    assert copy([65536, 65536]) == A.ERR_UNSUPPORTED
+    assert copy([limit + 1]) == A.ERR_UNSUPPORTED
+    assert copy([2, 2, 2 ** 62]) == A.ERR_UNSUPPORTED
+    assert copy([limit]) == A.ERR_NOT_INIT  # valid: the next step needs the context
+    assert copy([65536, 65535]) == A.ERR_NOT_INIT
+    assert copy([4, -1]) == A.ERR_DIM
+    assert copy([4, 4], base=None) == A.ERR_INVALID
+    assert copy([0, 5], base=None) == A.ERR_NOT_INIT  # empty views need no storage
+    sc = A.Scalar()
+    sc.dtype = A.F32
+    big = view([3, 6148914691236517206])
+    assert lib.phcu_fill(ctypes.byref(big), ctypes.byref(sc)) == A.ERR_UNSUPPORTED
+    prog = A.Program()
+    prog.n_instr, prog.out_type = 1, A.F32
+    prog.code[0].op, prog.code[0].src, prog.code[0].type, prog.code[0].btype = A.I_LD, 0, A.F32, A.F32
+    out = view([4])
+    assert lib.phcu_eval(ctypes.byref(prog), None, 1, ctypes.byref(out)) == A.ERR_INVALID  # no input array
+    prog.code[0].src = 1
+    ins = (A.View * 1)(view([4]))
+    assert lib.phcu_eval(ctypes.byref(prog), ins, 1, ctypes.byref(out)) == A.ERR_INVALID  # IN[1] of one input
+    prog.code[0].src = 0
+    assert lib.phcu_eval(ctypes.byref(prog), ins, 1, ctypes.byref(out)) == A.ERR_NOT_INIT
+
+
 def test_status_codes_and_enums_agree_with_oracle(ora):
     from phase_cu import _abi
 
