@@ -238,6 +238,15 @@ int32_t plan_reduce(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_
     return fail(PHCU_ERR_INVALID, "max/min output dtype must equal the input dtype");
   }
   if (axis >= in->rank) return fail(PHCU_ERR_INDEX, "axis %d is not present in a %d-dimensional array", axis, in->rank);
+  // the kernels write the output as one row-major run from its first element
+  // (check_view bounds the element count, so the running product stays small)
+  int64_t expect = 1;
+  for (int i = out->rank - 1; i >= 0 && view_size(out) > 0; i--) {
+    if (out->shape[i] != 1 && out->stride[i] != expect)
+      return fail(PHCU_ERR_INVALID, "reduction output must be contiguous and row-major (axis %d has stride %lld)", i,
+                  (long long)out->stride[i]);
+    expect *= out->shape[i];
+  }
 
   RedArgs& a = *pa;
   memset(&a, 0, sizeof(a));
@@ -358,11 +367,13 @@ int32_t plan_reduce(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_
 // scratch of `partial_cap` Partials; when null, scratch comes from the pool.
 int32_t reduce_impl(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_view_t* out, void* partial_buf,
                     size_t partial_cap) {
-  PHCU_TRY(require_ctx());
   RedArgs a;
   RedShape sh;
   bool trivial, empty_sum;
+  // planning checks the arguments and touches no device state, so it comes
+  // first and argument errors read the same with or without a context
   PHCU_TRY(plan_reduce(op, in, axis, out, (int64_t)ctx().sm_count * 1024, &a, &sh, &trivial, &empty_sum));
+  PHCU_TRY(require_ctx());
   if (trivial) return PHCU_OK;
   if (empty_sum) {
     phcu_scalar_t z;

@@ -350,6 +350,19 @@ def test_views_are_checked_before_the_device():
     assert lib.phcu_eval(ctypes.byref(prog), ins, 1, ctypes.byref(out)) == A.ERR_INVALID  # IN[1] of one input
     prog.code[0].src = 0
     assert lib.phcu_eval(ctypes.byref(prog), ins, 1, ctypes.byref(out)) == A.ERR_NOT_INIT
+    # reductions write their output as one row-major run: other layouts are refused
+    src = view([4, 6])
+    rev = view([4])
+    rev.offset, rev.stride[0] = 3, -1
+    assert lib.phcu_reduce(A.RED_SUM, ctypes.byref(src), 1, ctypes.byref(rev)) == A.ERR_INVALID
+    gap = view([2, 2])
+    gap.stride[0], gap.stride[1] = 4, 1
+    assert lib.phcu_reduce(A.RED_MAX, ctypes.byref(view([2, 2, 3])), 2, ctypes.byref(gap)) == A.ERR_INVALID
+    ones = view([4, 1])
+    ones.stride[1] = 7  # an axis of length one may have any stride
+    assert lib.phcu_reduce(A.RED_SUM, ctypes.byref(src), 1, ctypes.byref(ones)) == A.ERR_NOT_INIT
+    assert lib.phcu_reduce(A.RED_SUM, ctypes.byref(src), 1, ctypes.byref(view([4]))) == A.ERR_NOT_INIT
+    assert lib.phcu_reduce(A.RED_SUM, ctypes.byref(src), 1, ctypes.byref(view([5]))) == A.ERR_SHAPE
 
 
 def test_status_codes_and_enums_agree_with_oracle(ora):
