@@ -63,6 +63,9 @@ int32_t check_launch(const char* what);
 // exceeds the 48 KB default (only ever upwards, once per new maximum).
 int blocks_per_sm(const void* fn, int threads, size_t smem);
 
+// Destroys the heat runs' cached CUDA graphs (at shutdown).
+void release_heat_graphs();
+
 // stream-ordered scratch
 int32_t scratch_alloc(size_t bytes, void** p);
 void scratch_free(void* p);

@@ -237,22 +237,31 @@ static bool enqueue_heat_steps(T* u, T* tmp, int64_t n, int64_t m, T coef, int32
   return in_tmp;
 }
 
-static int32_t check_heat(const void* u, const void* o, int64_t n, int64_t m) {
-  PHCU_TRY(require_ctx());
+// Arguments of a heat call: two distinct, non-overlapping n x m grids of
+// `elem`-byte values.
+static int32_t check_heat(const void* u, const void* o, int64_t n, int64_t m, size_t elem) {
   if (!u || !o) return fail(PHCU_ERR_INVALID, "heat: null buffer");
-  if (u == o) return fail(PHCU_ERR_INVALID, "heat: input and output must differ");
   if (n < 1 || m < 1) return fail(PHCU_ERR_SHAPE, "heat: grid %lld x %lld", (long long)n, (long long)m);
   if ((n + HEAT_ROWS - 1) / HEAT_ROWS > 65535) return fail(PHCU_ERR_UNSUPPORTED, "heat: too many rows");
-  return PHCU_OK;
+  if (n > (INT64_MAX / (int64_t)elem) / m) return fail(PHCU_ERR_UNSUPPORTED, "heat: grid too large");
+  const uintptr_t bytes = (uintptr_t)(n * m) * elem, a = (uintptr_t)u, b = (uintptr_t)o;
+  if (a < b + bytes && b < a + bytes) return fail(PHCU_ERR_INVALID, "heat: input and output grids overlap");
+  return require_ctx();
 }
 
 // instantiated graphs of whole runs, keyed by their parameters
 using HeatKey = std::tuple<const void*, const void*, int64_t, int64_t, double, int, cudaStream_t, int>;
 static std::map<HeatKey, cudaGraphExec_t> g_heat_graphs;
 
+// Destroys the cached graphs (the context that instantiated them is going away).
+void release_heat_graphs() {
+  for (auto& kv : g_heat_graphs) cudaGraphExecDestroy(kv.second);
+  g_heat_graphs.clear();
+}
+
 template <typename T>
 static int32_t heat_run(T* u, T* tmp, int64_t n, int64_t m, T coef, int32_t steps, int32_t use_graph) {
-  PHCU_TRY(check_heat(u, tmp, n, m));
+  PHCU_TRY(check_heat(u, tmp, n, m, sizeof(T)));
   if (steps < 0) return fail(PHCU_ERR_INVALID, "heat: negative step count");
   if (steps == 0) return PHCU_OK;
   cudaStream_t s = stream();
@@ -295,7 +304,7 @@ using namespace phcu;
 extern "C" {
 
 int32_t phcu_heat_step(const float* u, float* out, int64_t n, int64_t m, float coef) {
-  PHCU_TRY(check_heat(u, out, n, m));
+  PHCU_TRY(check_heat(u, out, n, m, sizeof(float)));
   enqueue_heat<float>(u, out, n, m, coef, stream());
   count_launch();
   return check_launch("heat_step_kernel");

@@ -363,6 +363,14 @@ def test_views_are_checked_before_the_device():
     assert lib.phcu_reduce(A.RED_SUM, ctypes.byref(src), 1, ctypes.byref(ones)) == A.ERR_NOT_INIT
     assert lib.phcu_reduce(A.RED_SUM, ctypes.byref(src), 1, ctypes.byref(view([4]))) == A.ERR_NOT_INIT
     assert lib.phcu_reduce(A.RED_SUM, ctypes.byref(src), 1, ctypes.byref(view([5]))) == A.ERR_SHAPE
+    # heat grids: distinct, non-overlapping, n * m elements that fit the index arithmetic
+    heat = lib.phcu_heat_run
+    assert heat(0x10000, 0x10000 + 4 * 99, 10, 10, 0.2, 1, 0) == A.ERR_INVALID  # overlap by one element
+    assert heat(0x10000, 0x10000 + 4 * 100, 10, 10, 0.2, 1, 0) == A.ERR_NOT_INIT  # adjacent grids
+    assert heat(0x10000 + 4 * 100, 0x10000, 10, 10, 0.2, 1, 0) == A.ERR_NOT_INIT
+    assert heat(0x10000, 0x10000, 10, 10, 0.2, 1, 0) == A.ERR_INVALID
+    assert heat(0x10000, 0x20000, 2 ** 20, 2 ** 62, 0.2, 1, 0) == A.ERR_UNSUPPORTED
+    assert heat(0x10000, 0x20000, 0, 10, 0.2, 1, 0) == A.ERR_SHAPE
 
 
 def test_status_codes_and_enums_agree_with_oracle(ora):
