@@ -252,6 +252,7 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
                       Batch** out) {
   PHCU_TRY(require_ctx());
   if (n < 0 || (n > 0 && !tasks)) return fail(PHCU_ERR_INVALID, "batch: bad task list");
+  if (nprog < 0 || (nprog > 0 && !programs)) return fail(PHCU_ERR_INVALID, "batch: bad program table");
   Batch* b = new Batch();
   b->host_progs.assign(programs, programs + (programs ? nprog : 0));
   // program used for zero-filling empty sums
@@ -291,6 +292,7 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
       }
       int32_t rc = check_view(&t.out, "batch output");
       for (int k = 0; k < t.n_inputs && rc == PHCU_OK; k++) rc = check_view(&t.in[k], "batch input");
+      if (rc == PHCU_OK) rc = check_program(&programs[t.prog], t.n_inputs);
       if (rc == PHCU_OK && programs[t.prog].out_type != t.out.dtype)
         rc = fail(PHCU_ERR_INVALID, "batch task %d: program result type differs from the output", i);
       const phcu_view_t* ins[MAXIN];

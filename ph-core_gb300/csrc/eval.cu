@@ -119,7 +119,7 @@ int32_t launch_eval_plan(const EvalPlan& plan, const phcu_program_t& prog) {
 }
 
 // ------------------------------------------------------- program checks
-static int32_t check_program(const phcu_program_t* prog, int nin) {
+int32_t check_program(const phcu_program_t* prog, int nin) {
   if (!prog) return fail(PHCU_ERR_INVALID, "null program");
   if (prog->n_instr < 0 || prog->n_instr > PHCU_MAX_INSTR)
     return fail(PHCU_ERR_INVALID, "program length %d outside 0..%d", prog->n_instr, PHCU_MAX_INSTR);

@@ -38,5 +38,8 @@ bool views_overlap(const phcu_view_t* a, const phcu_view_t* b);
 bool views_identical(const phcu_view_t* a, const phcu_view_t* b);
 int32_t check_view(const phcu_view_t* v, const char* what);
 int64_t view_size(const phcu_view_t* v);
+// A program the interpreter can run with `nin` inputs: known opcodes and
+// types, operand sources that exist, valid conversion targets.
+int32_t check_program(const phcu_program_t* prog, int nin);
 
 }  // namespace phcu

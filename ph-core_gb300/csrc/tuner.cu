@@ -241,7 +241,11 @@ int32_t phcu_tune_measure(const phcu_task_t* task, const phcu_program_t* program
   cudaStream_t s = stream();
   cudaEvent_t e0, e1;
   PHCU_CUDA(cudaEventCreate(&e0));
-  PHCU_CUDA(cudaEventCreate(&e1));
+  const cudaError_t ce = cudaEventCreate(&e1);
+  if (ce != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return cuda_fail(ce, "cudaEventCreate(tune_measure)");
+  }
   int32_t rc = PHCU_OK;
   for (int c = 0; c < NCONF && rc == PHCU_OK; c++) {
     phcu_task_t t = *task;

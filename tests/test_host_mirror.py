@@ -363,6 +363,18 @@ def test_views_are_checked_before_the_device():
     assert lib.phcu_reduce(A.RED_SUM, ctypes.byref(src), 1, ctypes.byref(ones)) == A.ERR_NOT_INIT
     assert lib.phcu_reduce(A.RED_SUM, ctypes.byref(src), 1, ctypes.byref(view([4]))) == A.ERR_NOT_INIT
     assert lib.phcu_reduce(A.RED_SUM, ctypes.byref(src), 1, ctypes.byref(view([5]))) == A.ERR_SHAPE
+    # every program of the batched workload passes the library's program check
+    # (the batch executor refuses programs that fail it)
+    from phase_cu import batch
+
+    for k, p in enumerate(batch.program_table()):
+        t = A.F32 if k < 3 else A.I32
+        vs = (A.View * 2)(view([4]), view([4]))
+        for v in vs:
+            v.dtype = t
+        o = view([4])
+        o.dtype = t
+        assert lib.phcu_eval(ctypes.byref(p), vs, 2, ctypes.byref(o)) == A.ERR_NOT_INIT, k
     # heat grids: distinct, non-overlapping, n * m elements that fit the index arithmetic
     heat = lib.phcu_heat_run
     assert heat(0x10000, 0x10000 + 4 * 99, 10, 10, 0.2, 1, 0) == A.ERR_INVALID  # overlap by one element
