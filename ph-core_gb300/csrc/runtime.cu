@@ -176,6 +176,7 @@ int32_t phcu_set_stream(void* s) {
 
 int32_t phcu_get_stream(void** s) {
   PHCU_TRY(require_ctx());
+  if (!s) return fail(PHCU_ERR_INVALID, "phcu_get_stream: null output pointer");
   *s = (void*)g_ctx.stream;
   return PHCU_OK;
 }
@@ -196,6 +197,7 @@ int32_t phcu_last_error(char* buf, size_t len) {
 
 int32_t phcu_status_word(uint32_t* out, int32_t clear) {
   PHCU_TRY(require_ctx());
+  if (!out) return fail(PHCU_ERR_INVALID, "phcu_status_word: null output pointer");
   uint32_t v = 0;
   PHCU_CUDA(cudaMemcpyAsync(&v, g_ctx.status, sizeof(v), cudaMemcpyDeviceToHost, g_ctx.stream));
   PHCU_CUDA(cudaStreamSynchronize(g_ctx.stream));
@@ -208,6 +210,7 @@ int32_t phcu_status_word(uint32_t* out, int32_t clear) {
 }
 
 int32_t phcu_version(int32_t* major, int32_t* minor) {
+  if (!major || !minor) return fail(PHCU_ERR_INVALID, "phcu_version: null output pointer");
   *major = PHCU_VERSION_MAJOR;
   *minor = PHCU_VERSION_MINOR;
   return PHCU_OK;
@@ -318,7 +321,11 @@ int32_t phcu_graph_begin(void) {
 int32_t phcu_graph_end(void** graph_exec) {
   PHCU_TRY(require_ctx());
   cudaGraph_t g;
-  PHCU_CUDA(cudaStreamEndCapture(g_ctx.stream, &g));
+  PHCU_CUDA(cudaStreamEndCapture(g_ctx.stream, &g));  // the capture ends whatever follows
+  if (!graph_exec) {
+    cudaGraphDestroy(g);
+    return fail(PHCU_ERR_INVALID, "phcu_graph_end: null output pointer");
+  }
   cudaGraphExec_t ge;
   cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
   cudaGraphDestroy(g);
@@ -373,6 +380,7 @@ int32_t phcu_timer_stop(void* timer, float* ms) {
 }
 
 int32_t phcu_launch_count(uint64_t* n) {
+  if (!n) return fail(PHCU_ERR_INVALID, "phcu_launch_count: null output pointer");
   *n = g_ctx.launches;
   return PHCU_OK;
 }
