@@ -129,6 +129,11 @@ int32_t make_plan(const phcu_view_t* out, const phcu_view_t* const* ins, int nin
       if (shp[k][i] != shp[0][i])
         return fail(PHCU_ERR_SHAPE, "operand %d shape is not compatible with the output shape", k);
   }
+  // an output axis of stride 0 would have every one of its elements written
+  // to one place, by different threads
+  for (int i = 0; i < rk[0]; i++)
+    if (str[0][i] == 0) return fail(PHCU_ERR_INVALID, "the output view has stride 0 on an axis of extent %lld",
+                                    (long long)shp[0][i]);
   int rank = rk[0];
   Axis ax[MAXR];
   for (int i = 0; i < rank; i++) {
