@@ -4,7 +4,8 @@ the Python mirror's compile_program: instruction by instruction, immediates
 bit for bit, on fixed chains (the fused chain, stash use, Crystal's result
 types, checked and wrapping integer operators) and 4,000 random expression
 trees; CuProcView's operand views (sharing, index transforms) against
-hand-computed layouts.  Host logic only: compiled with g++, no GPU."""
+hand-computed layouts; the documented public surface compiles without
+warnings.  Host logic only: compiled with g++, no GPU."""
 import os
 import random
 import shutil
@@ -184,3 +185,17 @@ def test_random_expressions_match_the_python_compiler(exe):
     kinds = {x.split()[0] + ("" if x.startswith("ERR") else str(min(int(x.split()[2]), 8))) for x in expected}
     assert {"ERR", "P1", "P4", "P8"} <= kinds, kinds  # errors, single loads and long programs all occur
     assert sum(" 66 0 " in x for x in expected) > 50  # second stash register used
+
+
+@pytest.mark.parametrize("std", ["c++17", "c++20"])
+def test_public_surface_compiles_without_warnings(std):
+    """tests/host_cpp_api.cpp uses the surface INTEGRATION.md documents; its
+    static assertions pin Crystal's result types of fused chains."""
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    cmd = [gxx, "-std=" + std, "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
+           os.path.join(ROOT, "tests", "host_cpp_api.cpp"),
+           "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "ph-core_gb300", "host")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
