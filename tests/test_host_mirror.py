@@ -385,6 +385,34 @@ def test_views_are_checked_before_the_device():
     assert heat(0x10000, 0x20000, 0, 10, 0.2, 1, 0) == A.ERR_SHAPE
 
 
+def test_failed_init_leaves_nothing_behind():
+    """Without a usable GPU, phcu_init fails with the CUDA error and its
+    message, releases what it created and can be called again; every later
+    call still reports that there is no context."""
+    import __graft_entry__
+    from phase_cu import _abi as A
+
+    if not os.path.exists(os.path.join(ROOT, "ph-core_gb300", "phase_cu", "_lib", "libphcuda.so")):
+        __graft_entry__.build()
+    lib = A.load()
+    rc = lib.phcu_init(0)
+    if rc == A.OK:
+        lib.phcu_shutdown()
+        pytest.skip("a GPU is present: phcu_init succeeds")
+    assert rc in (A.ERR_CUDA, A.ERR_OOM)
+    assert "CUDA error" in A.last_error()
+    assert lib.phcu_init(0) == rc  # a second attempt fails the same way
+    v = A.View()
+    v.base, v.dtype, v.rank = 0x1000, A.F32, 1
+    v.shape[0], v.stride[0] = 4, 1
+    assert lib.phcu_copy(ctypes.byref(v), ctypes.byref(v)) == A.ERR_NOT_INIT
+    assert lib.phcu_shutdown() == A.OK
+    major, minor = ctypes.c_int32(), ctypes.c_int32()
+    assert lib.phcu_version(ctypes.byref(major), ctypes.byref(minor)) == A.OK and major.value >= 1
+    assert lib.phcu_version(None, None) == A.ERR_INVALID
+    assert lib.phcu_launch_count(None) == A.ERR_INVALID
+
+
 def test_status_codes_and_enums_agree_with_oracle(ora):
     from phase_cu import _abi
 
