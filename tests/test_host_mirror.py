@@ -396,8 +396,7 @@ def test_failed_init_leaves_nothing_behind():
         __graft_entry__.build()
     lib = A.load()
     rc = lib.phcu_init(0)
-    if rc == A.OK:
-        lib.phcu_shutdown()
+    if rc == A.OK:  # the context may serve other tests of this process: leave it
         pytest.skip("a GPU is present: phcu_init succeeds")
     assert rc in (A.ERR_CUDA, A.ERR_OOM)
     assert "CUDA error" in A.last_error()
