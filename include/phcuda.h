@@ -261,8 +261,8 @@ PHCU_API int32_t phcu_reduce(int32_t op, const phcu_view_t* in, int32_t axis, co
  * array of 2^18 partials (4 MiB) that every GPU loading the library holds
  * until the process exits; a reduction that would need more partials is
  * rejected with PHCU_ERR_UNSUPPORTED (phcu_reduce handles it).  The first call
- * on a device looks the array up (cudaGetSymbolAddress), so make that first
- * call before any stream capture.  Every call shares the array: calls that
+ * on a device after phcu_init looks the array up (cudaGetSymbolAddress), so
+ * make that first call before any stream capture.  Every call shares the array: calls that
  * overlap on the GPU (different streams, no ordering) race.  No call allocates
  * or frees memory. */
 PHCU_API int32_t phcu_reduce_noalloc(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_view_t* out);

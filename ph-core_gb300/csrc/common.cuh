@@ -66,6 +66,10 @@ int blocks_per_sm(const void* fn, int threads, size_t smem);
 // Destroys the heat runs' cached CUDA graphs (at shutdown).
 void release_heat_graphs();
 
+// Forgets the cached device addresses of the allocation-free reduction's
+// static scratch (at shutdown: a later context may load the module anew).
+void release_noalloc_scratch();
+
 // stream-ordered scratch
 int32_t scratch_alloc(size_t bytes, void** p);
 void scratch_free(void* p);

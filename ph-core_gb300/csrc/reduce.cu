@@ -408,8 +408,15 @@ constexpr size_t NOALLOC_PARTIALS = size_t(1) << 18;
 static __device__ __align__(256) Partial g_noalloc_partials[NOALLOC_PARTIALS];
 
 // Device address of g_noalloc_partials, looked up once per device (the host
-// symbol is only a stand-in: it must never be handed to a kernel).
+// symbol is only a stand-in: it must never be handed to a kernel).  Cleared
+// when the library's context is released: a device reset between
+// phcu_shutdown and the next phcu_init reloads the module, and the array may
+// then sit at another address.
 static void* g_noalloc_addr[64] = {nullptr};
+
+void release_noalloc_scratch() {
+  for (auto& p : g_noalloc_addr) p = nullptr;
+}
 
 static int32_t noalloc_scratch(void** out) {
   int dev = 0;

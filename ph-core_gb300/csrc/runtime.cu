@@ -101,6 +101,7 @@ static void release_context(Context& c) {
   if (c.d2h) cudaStreamSynchronize(c.d2h);
   if (c.h2d) cudaStreamSynchronize(c.h2d);
   release_heat_graphs();
+  release_noalloc_scratch();
   if (c.l2_scrub) cudaFree(c.l2_scrub);
   if (c.status) cudaFree(c.status);
   if (c.ev_work) cudaEventDestroy(c.ev_work);

@@ -1,5 +1,5 @@
 // Compile-only check of the C++ host mirror's public surface
-// (ph-core_gb300/host/phase.hpp), as INTEGRATION.md shows it: views,
+// (ph-core_gb300/host/phase.hpp) as a caller uses it: views,
 // eager operators with Crystal's result types, fused CuProcView chains,
 // reductions, chunk reads and writes, region operations.  The static
 // assertions pin the result types; tests/test_host_cpp_programs.py compiles
