@@ -16,6 +16,14 @@ from . import _abi as A
 from .narray import _Buffer, init, lib
 
 DEFAULT_CONFIG = 1  # 8192-element work items, planner's launch shape
+CHUNKS = (2048, 8192, 32768, 131072)  # work-item sizes (elements) of configurations c % 4
+
+
+def config_args(picks):
+    """(work-item sizes, layouts) of per-task configuration indices: config c
+    is work items of CHUNKS[c % 4] elements in layout c // 4 (0 = the
+    planner's launch shape, 1 = the alternative)."""
+    return [CHUNKS[int(c) % len(CHUNKS)] for c in picks], [int(c) // len(CHUNKS) for c in picks]
 
 
 def n_configs():
