@@ -78,6 +78,16 @@ enum {
 /* element types: Crystal Bool, Int32, Int64, Float32, Float64 */
 enum { PHCU_BOOL = 0, PHCU_I32 = 1, PHCU_I64 = 2, PHCU_F32 = 3, PHCU_F64 = 4 };
 
+/* An index operand: a phcu_view_t of this dtype is an input of phcu_eval (or
+ * of a batch task) whose element at view coordinate c is the Int32 value
+ * offset + sum_i c_i * stride[i], computed and never loaded (`base` is
+ * ignored and may be null).  Row-major strides of the output shape give each
+ * element's lexicographic index (the idx of NArray#map_with_index,
+ * src/n_array.cr:605-611); stride 1 on axis d and 0 elsewhere gives its
+ * coordinate along d (MultiIndexable#map_with_coord, src/multi_indexable.cr:708-712).
+ * In the program it is read as an Int32 input. */
+enum { PHCU_INDEX = 5 };
+
 /* infix operators (src/multi_indexable.cr:958-981) */
 enum {
   PHCU_OP_ADD = 0, PHCU_OP_SUB, PHCU_OP_MUL, PHCU_OP_DIV, PHCU_OP_FLOORDIV, PHCU_OP_MOD, PHCU_OP_POW,

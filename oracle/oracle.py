@@ -112,6 +112,9 @@ def _sigs():
         "ora_region_local_to_absolute": [_P(Region), _I64A, _I64A],
         "ora_xf_apply": [_P(Xf), _I64A, _I64A],
         "ora_gather": [_P(Operand), _vp, _i32],
+        "ora_gather_range": [_P(Operand), _vp, _i64, _i64, _i32],
+        "ora_map_binary_range": [_i32, _P(Operand), _P(Operand), _vp, _i64, _i64, _P(ctypes.c_uint32), _i32],
+        "ora_scatter_range": [_P(Operand), _P(Operand), _i64, _i64, _i32],
         "ora_narray_fetch_chunk": [_vp, _i32, _I64A, _i32, _P(Region), _vp, _i32],
         "ora_narray_set_chunk": [_vp, _i32, _I64A, _i32, _P(Region), _vp],
         "ora_narray_set_chunk_scalar": [_vp, _i32, _I64A, _i32, _P(Region), _vp],
@@ -372,6 +375,27 @@ def gather(v, nthreads=1):
     return out
 
 
+def gather_range(v, out, lo, hi, nthreads=1):
+    """Elements [lo, hi) of gather(v), written into `out` (a bounded sample of
+    the full-size gather)."""
+    _chk(lib().ora_gather_range(ctypes.byref(v.op), out.ctypes.data, lo, hi, nthreads), "gather_range")
+    return out
+
+
+def map_binary_range(op, a, b, out, lo, hi, nthreads=1):
+    """Elements [lo, hi) of map_binary(op, a, b), written into `out`."""
+    st = ctypes.c_uint32()
+    _chk(lib().ora_map_binary_range(op, ctypes.byref(a.op), ctypes.byref(b.op), out.ctypes.data, lo, hi,
+                                    ctypes.byref(st), nthreads), "map_binary_range")
+    return out, st.value
+
+
+def scatter_range(dst, src, lo, hi, nthreads=1):
+    """Writes [lo, hi) of scatter(dst, src), for a source that does not alias dst."""
+    _chk(lib().ora_scatter_range(ctypes.byref(dst.op), ctypes.byref(src.op), lo, hi, nthreads), "scatter_range")
+    return dst.arr
+
+
 def narray_fetch_chunk(arr, lits, drop=True, nthreads=1):
     """NArray#[] via IndexRegion + the buffer-index odometer (n_array.cr:450-453)."""
     arr = np.ascontiguousarray(arr)
@@ -465,6 +489,21 @@ def concatenate(narrs, axis=0):
             values.extend(flats[i][pos[i]:pos[i] + size].tolist())
             pos[i] += size
     return np.array(values, dtype=first.dtype).reshape(shape)
+
+
+def lex_index(shape):
+    """The index NArray#map_with_index hands its block (n_array.cr:605-611,
+    `@buffer.map_with_index`): the buffer position of every element, which for
+    the row-major buffer is its lexicographic position (Int32)."""
+    n = int(np.prod(shape, dtype=np.int64))
+    return np.arange(n, dtype=np.int32).reshape(shape)
+
+
+def coords(shape):
+    """The coordinates LexIterator.cover(shape) yields in lexicographic order
+    (n_array.cr:641-650; MultiIndexable#map_with_coord builds over them,
+    multi_indexable.cr:708-712): one Int32 array per axis."""
+    return [np.ascontiguousarray(c.astype(np.int32)) for c in np.indices(shape, dtype=np.int64)]
 
 
 def result_dtype(op, ta, tb):

@@ -291,7 +291,7 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
         return fail(PHCU_ERR_INVALID, "batch task %d: %d inputs", i, t.n_inputs);
       }
       int32_t rc = check_view(&t.out, "batch output");
-      for (int k = 0; k < t.n_inputs && rc == PHCU_OK; k++) rc = check_view(&t.in[k], "batch input");
+      for (int k = 0; k < t.n_inputs && rc == PHCU_OK; k++) rc = check_input_view(&t.in[k], "batch input");
       if (rc == PHCU_OK) rc = check_program(&programs[t.prog], t.n_inputs);
       if (rc == PHCU_OK && programs[t.prog].out_type != t.out.dtype)
         rc = fail(PHCU_ERR_INVALID, "batch task %d: program result type differs from the output", i);

@@ -152,6 +152,7 @@ enum VMode : int32_t {
   VM_SCALAR = 0,   // scalar loads/stores with the canonical inner stride
   VM_VEC = 1,      // inner stride +1 and aligned: vector access
   VM_VEC_REV = 2,  // inner stride -1 and aligned at the low end: reversed vector access
+  VM_INDEX = 3,    // an index operand (PHCU_INDEX): the value is computed, base holds its offset
 };
 
 }  // namespace phcu

@@ -150,7 +150,7 @@ int32_t eval_views(const phcu_program_t* prog, const phcu_view_t* inputs, int ni
   PHCU_TRY(check_view(out, "output"));
   if (nin < 0 || nin > MAXIN) return fail(PHCU_ERR_INVALID, "n_inputs %d outside 0..%d", nin, MAXIN);
   if (nin > 0 && !inputs) return fail(PHCU_ERR_INVALID, "null input array");
-  for (int k = 0; k < nin; k++) PHCU_TRY(check_view(&inputs[k], "input"));
+  for (int k = 0; k < nin; k++) PHCU_TRY(check_input_view(&inputs[k], "input"));
   PHCU_TRY(check_program(prog, nin));
   if (prog->out_type != out->dtype)
     return fail(PHCU_ERR_INVALID, "program result type %d differs from output dtype %d", prog->out_type, out->dtype);

@@ -59,6 +59,16 @@ __device__ __forceinline__ void row_group(const EvalPlan& p, const phcu_program_
     const char* base = p.in[k].base;
     const int64_t sw = p.in[k].stride[W];
     const int vm = p.in[k].vmode;
+    if constexpr (interpreted(FAST)) {
+      if (vm == VM_INDEX) {  // an index operand: Int32 value offset + coordinate . stride
+        const int64_t i0 = (int64_t)(uintptr_t)base;
+#pragma unroll
+        for (int u = 0; u < U; u++)
+#pragma unroll
+          for (int i = 0; i < VEC; i++) in[k][u * VEC + i] = (S)(uint32_t)(i0 + off_in[k][u] + (int64_t)i * sw);
+        continue;
+      }
+    }
     switch (dtype_size(p.in[k].dtype)) {
       case 4:
 #pragma unroll
@@ -388,8 +398,14 @@ inline bool program_uses_stash(const phcu_program_t& P) {
 // A plain move: one input, one LD of its own type into an output of that type.
 // [ACC = IN0 (its own type); ACC = ACC op IN1 (IN1 already of the compute
 // type, or an integer exponent); optional CVT]: runs in place (run_binop).
+inline bool plan_has_index(const EvalPlan& plan) {
+  for (int k = 0; k < plan.nin; k++)
+    if (plan.in[k].vmode == VM_INDEX) return true;
+  return false;
+}
+
 inline bool program_is_binop(const phcu_program_t& P, const EvalPlan& plan) {
-  if (plan.nin != 2 || P.n_instr < 2 || P.n_instr > 3) return false;
+  if (plan.nin != 2 || P.n_instr < 2 || P.n_instr > 3 || plan_has_index(plan)) return false;
   const phcu_instr_t& a = P.code[0];
   const phcu_instr_t& b = P.code[1];
   if (a.op != PHCU_I_LD || a.src != 0 || a.type != a.btype || a.type != plan.in[0].dtype) return false;
@@ -402,7 +418,7 @@ inline bool program_is_binop(const phcu_program_t& P, const EvalPlan& plan) {
 }
 
 inline bool program_is_copy(const phcu_program_t& P, const EvalPlan& plan) {
-  return plan.nin == 1 && P.n_instr == 1 && P.code[0].op == PHCU_I_LD && P.code[0].src == 0 &&
+  return plan.nin == 1 && !plan_has_index(plan) && P.n_instr == 1 && P.code[0].op == PHCU_I_LD && P.code[0].src == 0 &&
          P.code[0].type == P.code[0].btype && P.code[0].type == plan.in[0].dtype && P.out_type == plan.out.dtype &&
          plan.in[0].dtype == plan.out.dtype;
 }

@@ -48,6 +48,15 @@ int32_t check_view(const phcu_view_t* v, const char* what) {
   return PHCU_OK;
 }
 
+int32_t check_input_view(const phcu_view_t* v, const char* what) {
+  if (!is_index_view(v)) return check_view(v, what);
+  // an index operand: the shape rules of check_view, no storage
+  phcu_view_t t = *v;
+  t.dtype = PHCU_I32;
+  t.base = (void*)&t;  // any non-null address: it is never read
+  return check_view(&t, what);
+}
+
 void view_extent(const phcu_view_t* v, uintptr_t* lo, uintptr_t* hi) {
   int es = dtype_size(v->dtype);
   int64_t mn = v->offset, mx = v->offset;
@@ -61,6 +70,7 @@ void view_extent(const phcu_view_t* v, uintptr_t* lo, uintptr_t* hi) {
 }
 
 bool views_overlap(const phcu_view_t* a, const phcu_view_t* b) {
+  if (is_index_view(a) || is_index_view(b)) return false;  // index operands have no storage
   uintptr_t al, ah, bl, bh;
   view_extent(a, &al, &ah);
   view_extent(b, &bl, &bh);
@@ -188,7 +198,18 @@ int32_t make_plan(const phcu_view_t* out, const phcu_view_t* const* ins, int nin
   Operand* dst[MAXIN + 1];
   dst[0] = &p->out;
   for (int k = 0; k < nin; k++) dst[k + 1] = &p->in[k];
+  bool any_index = false;
   for (int k = 0; k < nops; k++) {
+    if (is_index_view(ops[k])) {
+      // an index operand: the value of canonical element 0 travels in `base`
+      any_index = true;
+      dst[k]->base = (const char*)(uintptr_t)off[k];
+      dst[k]->dtype = PHCU_I32;
+      for (int i = 0; i < r; i++) dst[k]->stride[i] = m[i].st[k];
+      for (int i = r; i < MAXR; i++) dst[k]->stride[i] = 0;
+      dst[k]->vmode = VM_INDEX;
+      continue;
+    }
     int es = dtype_size(ops[k]->dtype);
     dst[k]->base = (const char*)ops[k]->base + off[k] * es;
     dst[k]->dtype = ops[k]->dtype;
@@ -203,7 +224,8 @@ int32_t make_plan(const phcu_view_t* out, const phcu_view_t* const* ins, int nin
   int mode = MODE_ROW;
   int raxis = -1;
   uint32_t staged = 0;
-  if (r >= 2 && p->out.stride[W] == 1 && m[W].n >= 8) {
+  // index operands are computed by the ROW body only
+  if (!any_index && r >= 2 && p->out.stride[W] == 1 && m[W].n >= 8) {
     // candidate inputs: contiguous along some other axis R, far apart along W
     int best = -1;
     int64_t best_bytes = 0;
@@ -226,7 +248,7 @@ int32_t make_plan(const phcu_view_t* out, const phcu_view_t* const* ins, int nin
     }
   }
   if (force_mode == MODE_ROW) mode = MODE_ROW;
-  if (force_mode == MODE_TILE && raxis >= 0) mode = MODE_TILE;
+  if (force_mode == MODE_TILE && raxis >= 0 && !any_index) mode = MODE_TILE;
 
   if (mode == MODE_TILE) {
     p->mode = MODE_TILE;
@@ -266,7 +288,7 @@ int32_t make_plan(const phcu_view_t* out, const phcu_view_t* const* ins, int nin
     bool all = true;
     for (int k = 0; k < nops; k++) {
       const int64_t sw = dst[k]->stride[W];
-      if ((sw == 1 || sw == -1) && !vec_ok(dst[k], v)) all = false;
+      if (dst[k]->vmode != VM_INDEX && (sw == 1 || sw == -1) && !vec_ok(dst[k], v)) all = false;
     }
     if (all) {
       vec = v;
@@ -278,7 +300,7 @@ int32_t make_plan(const phcu_view_t* out, const phcu_view_t* const* ins, int nin
   for (int k = 0; k < nops; k++) {
     Operand* o = dst[k];
     const int64_t sw = o->stride[W];
-    if (vec == 1 || (sw != 1 && sw != -1)) continue;
+    if (o->vmode == VM_INDEX || vec == 1 || (sw != 1 && sw != -1)) continue;
     // an operand aligned for `vec` is also aligned for the 4-element chunks a
     // kernel may use instead of 8
     if (vec_ok(o, vec)) o->vmode = (sw == 1) ? VM_VEC : VM_VEC_REV;

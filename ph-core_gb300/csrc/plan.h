@@ -37,6 +37,10 @@ void view_extent(const phcu_view_t* v, uintptr_t* lo, uintptr_t* hi);
 bool views_overlap(const phcu_view_t* a, const phcu_view_t* b);
 bool views_identical(const phcu_view_t* a, const phcu_view_t* b);
 int32_t check_view(const phcu_view_t* v, const char* what);
+// check_view for an input of an elementwise program: also accepts an index
+// operand (dtype PHCU_INDEX, base ignored).
+int32_t check_input_view(const phcu_view_t* v, const char* what);
+inline bool is_index_view(const phcu_view_t* v) { return v && v->dtype == PHCU_INDEX; }
 int64_t view_size(const phcu_view_t* v);
 // A program the interpreter can run with `nin` inputs: known opcodes and
 // types, operand sources that exist, valid conversion targets.

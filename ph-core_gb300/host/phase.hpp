@@ -935,6 +935,106 @@ struct Leaf {
   }
 };
 
+inline size_t type_bytes(int32_t t) { return t == PHCU_BOOL ? 1 : (t == PHCU_I64 || t == PHCU_F64) ? 8 : 4; }
+
+inline void leaf_slots(const Expr& e, std::vector<int32_t>& acc) {
+  if (e.kind == Expr::IN) {
+    if (std::find(acc.begin(), acc.end(), e.slot) == acc.end()) acc.push_back(e.slot);
+    return;
+  }
+  if (e.a) leaf_slots(*e.a, acc);
+  if (e.b) leaf_slots(*e.b, acc);
+}
+
+inline int expr_size(const Expr& e) {
+  if (e.kind == Expr::IN || e.kind == Expr::CONST) return 0;
+  return 1 + (e.a ? expr_size(*e.a) : 0) + (e.b ? expr_size(*e.b) : 0);
+}
+
+// Whether an expression over `nleaves` views compiles into one program.
+inline bool fits(const ExprP& e, size_t nleaves, int32_t out_type) {
+  if (nleaves > (size_t)PHCU_MAX_INPUTS) return false;
+  try {
+    compile_program(e, out_type, nullptr);
+  } catch (const NotImplementedError&) {
+    return false;
+  }
+  return true;
+}
+
+inline void operator_nodes(const ExprP& e, std::vector<ExprP>& acc) {
+  for (const ExprP* c : {&e->a, &e->b}) {
+    if (!*c) continue;
+    if ((*c)->kind == Expr::BIN || (*c)->kind == Expr::UN) acc.push_back(*c);
+    operator_nodes(*c, acc);
+  }
+}
+
+inline ExprP replace_node(const ExprP& e, const Expr* old, const ExprP& with) {
+  if (e.get() == old) return with;
+  if (e->kind == Expr::IN || e->kind == Expr::CONST) return e;
+  auto n = std::make_shared<Expr>(*e);
+  if (e->a) n->a = replace_node(e->a, old, with);
+  if (e->b) n->b = replace_node(e->b, old, with);
+  return n;
+}
+
+// Splits an expression that one device program cannot hold (more than
+// PHCU_MAX_INPUTS distinct views, more than PHCU_MAX_INSTR instructions, or
+// nesting deeper than the two stash registers): the largest operator
+// sub-expression that fits is evaluated into a temporary array of its own
+// type, which becomes a new leaf, until the rest fits.  ProcView composes
+// without limit (proc_view.cr:32-35); every operator still runs once per
+// element in its own type, so the results equal the unsplit expression's.
+// `raises` collects whether any piece can set the status word.
+inline void split_to_fit(std::vector<Leaf>& leaves, ExprP& expr, const std::vector<int64_t>& shape,
+                         int32_t out_type, bool* raises) {
+  for (;;) {
+    std::vector<int32_t> used;
+    leaf_slots(*expr, used);
+    if (fits(expr, used.size(), out_type)) break;
+    std::vector<ExprP> nodes;
+    operator_nodes(expr, nodes);
+    ExprP best;
+    for (const ExprP& n : nodes) {
+      std::vector<int32_t> ids;
+      leaf_slots(*n, ids);
+      if (fits(n, ids.size(), n->t) && (!best || expr_size(*n) > expr_size(*best))) best = n;
+    }
+    if (!best) throw NotImplementedError("expression cannot be split into device programs");
+    // the piece over its own leaves
+    std::vector<int32_t> ids;
+    leaf_slots(*best, ids);
+    std::sort(ids.begin(), ids.end());
+    ExprP piece = relabel(best, [&ids](int32_t k) {
+      return (int32_t)(std::lower_bound(ids.begin(), ids.end(), k) - ids.begin());
+    });
+    bool r = false;
+    const phcu_program_t p = compile_program(piece, best->t, &r);
+    if (raises) *raises = *raises || r;
+    const int64_t n = shape_to_size(shape);
+    Leaf tmp{std::make_shared<Buffer>((size_t)std::max<int64_t>(n, 1) * type_bytes(best->t)),
+             Affine{0, shape, row_major(shape)}, best->t};
+    phcu_view_t ins[PHCU_MAX_INPUTS];
+    std::memset(ins, 0, sizeof(ins));
+    for (size_t k = 0; k < ids.size(); k++) ins[k] = leaves[(size_t)ids[k]].desc();
+    const phcu_view_t o = tmp.desc();
+    check(phcu_eval(&p, ins, (int32_t)ids.size(), &o), "phcu_eval");
+    leaves.push_back(tmp);
+    expr = replace_node(expr, best.get(), input((int32_t)leaves.size() - 1, best->t));
+    // drop the leaves nothing reads any more
+    std::vector<int32_t> keep;
+    leaf_slots(*expr, keep);
+    std::sort(keep.begin(), keep.end());
+    std::vector<Leaf> kept;
+    for (int32_t k : keep) kept.push_back(leaves[(size_t)k]);
+    expr = relabel(expr, [&keep](int32_t k) {
+      return (int32_t)(std::lower_bound(keep.begin(), keep.end(), k) - keep.begin());
+    });
+    leaves = std::move(kept);
+  }
+}
+
 inline std::string shape_text(const std::vector<int64_t>& s) {
   std::string t = "[";
   for (size_t i = 0; i < s.size(); i++) t += (i ? ", " : "") + std::to_string(s[i]);
@@ -1018,19 +1118,22 @@ class CuProcView {
     return detail::compile_program(expr_, DType<T>::id, raises);
   }
 
-  // One phcu_eval into a new contiguous array.
+  // One phcu_eval into a new contiguous array (more than one when the
+  // expression is larger than one device program: see detail::split_to_fit).
   CuNArray<T> to_cu() const {
-    if (leaves_.size() > (size_t)PHCU_MAX_INPUTS)
-      throw NotImplementedError("a fused program reads at most " + std::to_string(PHCU_MAX_INPUTS) +
-                                " distinct views");
     bool raises = false;
-    const phcu_program_t p = program(&raises);
+    std::vector<detail::Leaf> leaves = leaves_;
+    detail::ExprP expr = expr_;
+    detail::split_to_fit(leaves, expr, shape_, DType<T>::id, &raises);
+    bool r = false;
+    const phcu_program_t p = detail::compile_program(expr, DType<T>::id, &r);
+    raises = raises || r;
     CuNArray<T> out(shape_);
     phcu_view_t ins[PHCU_MAX_INPUTS];
     std::memset(ins, 0, sizeof(ins));
-    for (size_t k = 0; k < leaves_.size(); k++) ins[k] = leaves_[k].desc();
+    for (size_t k = 0; k < leaves.size(); k++) ins[k] = leaves[k].desc();
     const phcu_view_t o = out.desc();
-    check(phcu_eval(&p, ins, (int32_t)leaves_.size(), &o), "phcu_eval");
+    check(phcu_eval(&p, ins, (int32_t)leaves.size(), &o), "phcu_eval");
     if (raises) check_status();
     return out;
   }

@@ -17,6 +17,8 @@ MAX_INSTR = 24
 BOOL, I32, I64, F32, F64 = 0, 1, 2, 3, 4
 DTYPE_NAMES = {BOOL: "Bool", I32: "Int32", I64: "Int64", F32: "Float32", F64: "Float64"}
 DTYPE_SIZE = {BOOL: 1, I32: 4, I64: 8, F32: 4, F64: 8}
+# an index operand (an input whose Int32 value is offset + coordinate . stride)
+INDEX = 5
 
 # status codes
 OK = 0

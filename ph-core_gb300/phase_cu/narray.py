@@ -423,6 +423,109 @@ class _Indexable:
         pv = CuProcView._leaf(self)
         return pv.process(fn) if fn is not None else pv
 
+    def _as_leaf(self):
+        """This operand as a read-only CuView leaf of a program."""
+        buf, off, shape, stride = self._desc()
+        return CuView(self._base(), buf, self.dtype, off, shape, stride)
+
+    def _as_proc(self):
+        return self if isinstance(self, CuProcView) else CuProcView._leaf(self)
+
+    def process_with_index(self, fn):
+        """Lazy form of map_with_index: fn(element, index) with the element's
+        lexicographic index as an Int32 symbol (an index operand computed on the
+        device, never stored)."""
+        pv = self._as_proc()
+        idx = CuIndexView.lex(self.shape)
+        leaves = list(pv._leaves) + [idx]
+        out = fn(_Sym(pv._expr, pv.dtype), _Sym(("in", len(leaves) - 1, A.I32), A.I32))
+        return CuProcView._of_result(leaves, out, self.shape)
+
+    def process_with_coord(self, fn):
+        """Lazy form of map_with_coord: fn(element, coord), coord a list of
+        Int32 symbols, one per axis (index operands computed on the device)."""
+        pv = self._as_proc()
+        leaves = list(pv._leaves)
+        coord = []
+        for d in range(self.dimensions):
+            leaves.append(CuIndexView.axis(self.shape, d))
+            coord.append(_Sym(("in", len(leaves) - 1, A.I32), A.I32))
+        out = fn(_Sym(pv._expr, pv.dtype), coord)
+        return CuProcView._of_result(leaves, out, self.shape)
+
+    def map(self, fn):
+        """MultiIndexable#map / NArray#map (multi_indexable.cr:722-726,
+        n_array.cr:589-595): a new array of fn(element), one kernel."""
+        return self.process(fn).to_cu()
+
+    def map_with_index(self, fn):
+        """NArray#map_with_index (n_array.cr:605-611): a new array of
+        fn(element, lexicographic index), one kernel."""
+        return self.process_with_index(fn).to_cu()
+
+    def map_with_coord(self, fn):
+        """MultiIndexable#map_with_coord (multi_indexable.cr:708-712,
+        n_array.cr:614-618): a new array of fn(element, coord), one kernel."""
+        return self.process_with_coord(fn).to_cu()
+
+    def process_with(self, *args):
+        """Lazy form of map_with: the last argument is the block, called with
+        this element and the elements of every MultiIndexable argument (scalar
+        arguments are passed as they are)."""
+        *others, fn = args
+        if not callable(fn):
+            raise ArgumentError("map_with: the last argument must be the block")
+        pv = self._as_proc()
+        leaves = list(pv._leaves)
+        syms = []
+        for o in others:
+            if isinstance(o, _Indexable):
+                if o.shape != self.shape:
+                    raise ShapeError("The shape of this MultiIndexable (%r) does not match the shape of the one "
+                                     "provided (%r), so 'map_with' cannot be applied element-wise."
+                                     % (self.shape, o.shape))
+                op = o._as_proc()
+                base = len(leaves)
+                leaves += op._leaves
+                syms.append(_Sym(_shift(op._expr, base), op.dtype))
+            else:
+                syms.append(o)
+        out = fn(_Sym(pv._expr, pv.dtype), *syms)
+        return CuProcView._of_result(leaves, out, self.shape)
+
+    def map_with(self, *args):
+        """MultiIndexable#map_with (multi_indexable.cr:1026-1078): a new array of
+        fn(element, *argument elements); the last argument is the block."""
+        return self.process_with(*args).to_cu()
+
+    # in-place forms (Mutable#map!, #map_with!, #map_with_coord!; NArray#map_with_index!)
+    def _write_self(self, pv):
+        if not isinstance(self, (CuNArray, CuMutableView)):
+            raise NotImplementedError("%s is read-only: in-place maps need a CuNArray or a CuMutableView"
+                                      % type(self).__name__)
+        out = self._cview()
+        pv._eval_into(out, self.dtype)
+        return self
+
+    def map_inplace(self, fn):
+        """Mutable#map! / NArray#map! (mutable.cr:29-33, n_array.cr:621-627):
+        self = fn(self), one kernel."""
+        return self._write_self(self.process(fn))
+
+    def map_with_index_inplace(self, fn):
+        """NArray#map_with_index! (n_array.cr:631-637): self = fn(self, index)."""
+        return self._write_self(self.process_with_index(fn))
+
+    def map_with_coord_inplace(self, fn):
+        """Mutable#map_with_coord! / NArray#map_with_coord! (mutable.cr:16-20,
+        n_array.cr:641-650): self = fn(self, coord)."""
+        return self._write_self(self.process_with_coord(fn))
+
+    def map_with_inplace(self, *args):
+        """Mutable#map_with! (mutable.cr:54-67): self = fn(self, *argument
+        elements); the last argument is the block."""
+        return self._write_self(self.process_with(*args))
+
     # --------------------------------------------------- iteration (host)
     def each(self):
         return iter(self.to_narr().reshape(-1).tolist())
@@ -940,11 +1043,6 @@ class CuNArray(_Indexable):
         lits = normalise_literal(region)
         return v._restrict(lits) if lits else v
 
-    def map_inplace(self, fn):
-        """Mutable#map! with a symbolic block: self = fn(self), one kernel."""
-        pv = CuProcView._leaf(self).process(fn)
-        pv._eval_into(self._view(), self.dtype)
-        return self
 
 
 def _write_region(target, region, src):
@@ -1128,6 +1226,53 @@ class CuMutableView(CuView):
     set_mask = CuNArray.set_mask
 
 
+class CuIndexView(CuView):
+    """An index operand: a read-only Int32 "array" whose element at coordinate
+    c is offset + sum c_i * stride_i, computed on the device (PHCU_INDEX) and
+    never stored.  CuIndexView.lex(shape) holds every element's lexicographic
+    index, CuIndexView.axis(shape, d) its coordinate along axis d.  Views of it
+    (regions, permutations, reversals) fold into the affine map like any view,
+    so an index keeps naming the element it was computed for."""
+
+    def __init__(self, offset, shape, stride):
+        super().__init__(None, None, A.I32, offset, shape, stride)
+
+    @classmethod
+    def lex(cls, shape):
+        return cls(0, list(shape), _row_major(list(shape)))
+
+    @classmethod
+    def axis(cls, shape, d):
+        return cls(0, list(shape), [1 if i == d else 0 for i in range(len(shape))])
+
+    def _new(self, off, shape, stride):
+        return CuIndexView(off, shape, stride)
+
+    def _as_leaf(self):
+        return self.clone()
+
+    def _cview(self):
+        return _make_view(None, A.INDEX, self._off, self._shape, self._stride)
+
+    def view(self, *region):
+        lits = normalise_literal(region)
+        v = self.clone()
+        return v._restrict(lits) if lits else v
+
+    def _unsafe_fetch_chunk(self, region):
+        return self._new(*_affine_region(self._off, self._shape, self._stride, region))
+
+    def reshape(self, *new_shape):
+        new_shape = [int(x) for x in normalise_literal(new_shape)]
+        r = _affine_reshape(self._off, self._shape, self._stride, new_shape)
+        if r is None or shape_to_size(new_shape) != self.size:
+            return self.to_cu().reshape(new_shape)
+        return self._new(*r)
+
+    def to_cu(self):
+        return CuProcView._leaf(self).to_cu()
+
+
 # ============================================================= CuProcView
 class _Sym:
     """Symbolic element handed to process() blocks."""
@@ -1186,9 +1331,25 @@ class CuProcView(_Indexable):
     def _leaf(cls, x):
         if isinstance(x, CuProcView):
             return x
-        buf, off, shape, stride = x._desc()
-        v = CuView(x._base(), buf, x.dtype, off, shape, stride)
-        return cls([v], ("in", 0, x.dtype), x.dtype, x.shape)
+        return cls([x._as_leaf()], ("in", 0, x.dtype), x.dtype, x.shape)
+
+    @classmethod
+    def _of_result(cls, leaves, out, shape):
+        """The program whose result is `out` (a symbol, or a constant the block
+        returned), keeping only the leaves it reads."""
+        if isinstance(out, _Sym):
+            pv = cls(leaves, out.expr, out.dtype, shape)
+        else:
+            t = scalar_dtype(out)
+            pv = cls(leaves, ("const", out, t), t, shape)
+        return pv._prune()._dedupe()
+
+    def _prune(self):
+        used = sorted(_leaf_ids(self._expr))
+        remap = {old: new for new, old in enumerate(used)}
+        self._expr = _remap(self._expr, remap)
+        self._leaves = [self._leaves[i] for i in used]
+        return self
 
     def _desc(self):
         raise NotImplementedError("a CuProcView has no storage; materialise it with to_cu()")
@@ -1243,8 +1404,7 @@ class CuProcView(_Indexable):
                 raise ShapeError("The shape of this MultiIndexable (%r) does not match the shape of the one provided "
                                  "(%r), so '%s' cannot be applied element-wise." % (self._shape, other.shape,
                                                                                      _OP_NAMES.get(op)))
-            buf, off, shape, stride = other._desc()
-            leaves.append(CuView(other._base(), buf, other.dtype, off, shape, stride))
+            leaves.append(other._as_leaf())
             oe = ("in", len(leaves) - 1, other.dtype)
             ot = other.dtype
         else:
@@ -1259,7 +1419,8 @@ class CuProcView(_Indexable):
         # identical leaf views share one input slot
         keys, remap, leaves = {}, {}, []
         for i, l in enumerate(self._leaves):
-            k = (l._buf.ptr if l._buf else 0, l.dtype, l._off, tuple(l._shape), tuple(l._stride))
+            k = ("index" if isinstance(l, CuIndexView) else l._buf.ptr if l._buf else 0, l.dtype, l._off,
+                 tuple(l._shape), tuple(l._stride))
             if k not in keys:
                 keys[k] = len(leaves)
                 leaves.append(l)
@@ -1274,16 +1435,22 @@ class CuProcView(_Indexable):
 
     # ------------------------------------------------------------- evaluate
     def _eval_into(self, out_view, out_dtype):
-        expr = self._expr
-        leaves = self._leaves
-        if len(leaves) > A.MAX_INPUTS:
-            raise NotImplementedError("a fused program reads at most %d distinct views" % A.MAX_INPUTS)
-        prog, can_raise = compile_program(expr, out_dtype)
+        """Runs the program into out_view.  An expression the device program
+        cannot hold in one piece (more than MAX_INPUTS distinct views, more
+        than MAX_INSTR instructions, or nesting deeper than the two stash
+        registers) is split: its largest sub-expression that fits is
+        materialised into a temporary array of its own type, which becomes a
+        leaf, until the rest fits (ProcView composes without limit,
+        proc_view.cr:32-35).  Every operation still runs once per element in
+        its own type, so the results are those of the unsplit expression."""
+        expr, leaves, temps, can_raise = _split_to_fit(self._expr, list(self._leaves), self._shape, out_dtype)
+        prog, raises = compile_program(expr, out_dtype)
         ins = (A.View * max(1, len(leaves)))()
         for k, l in enumerate(leaves):
             ins[k] = l._cview()
         A.check(lib().phcu_eval(ctypes.byref(prog), ins, len(leaves), ctypes.byref(out_view)), "phcu_eval")
-        if can_raise and config.eager_errors:
+        del temps  # freed stream-ordered, after the launch that reads them
+        if (can_raise or raises) and config.eager_errors:
             check_errors()
 
     def to_cu(self):
@@ -1311,6 +1478,99 @@ def _shift(e, base):
     if k == "cvt":
         return ("cvt", e[1], _shift(e[2], base))
     return e
+
+
+def _fits(expr, nleaves, out_dtype):
+    if nleaves > A.MAX_INPUTS:
+        return False
+    try:
+        compile_program(expr, out_dtype)
+    except NotImplementedError:
+        return False
+    return True
+
+
+def _subtrees(e, acc):
+    """Every operator node below the root (with repeats)."""
+    k = e[0]
+    if k == "bin":
+        for c in (e[2], e[3]):
+            if c[0] in ("bin", "un", "cvt"):
+                acc.append(c)
+            _subtrees(c, acc)
+    elif k in ("un", "cvt"):
+        c = e[2]
+        if c[0] in ("bin", "un", "cvt"):
+            acc.append(c)
+        _subtrees(c, acc)
+    return acc
+
+
+def _size(e):
+    k = e[0]
+    if k == "bin":
+        return 1 + _size(e[2]) + _size(e[3])
+    if k in ("un", "cvt"):
+        return 1 + _size(e[2])
+    return 0
+
+
+def _replace(e, old, new):
+    if e == old:
+        return new
+    k = e[0]
+    if k == "bin":
+        return ("bin", e[1], _replace(e[2], old, new), _replace(e[3], old, new)) + tuple(e[4:])
+    if k == "un":
+        return ("un", e[1], _replace(e[2], old, new), e[3])
+    if k == "cvt":
+        return ("cvt", e[1], _replace(e[2], old, new))
+    return e
+
+
+def _split_to_fit(expr, leaves, shape, out_dtype):
+    """Materialises sub-expressions of `expr` until it fits one device program.
+    Returns (expr, leaves, temporaries, can_raise)."""
+    temps = []
+    can_raise = False
+    while not _fits(expr, len(_leaf_ids(expr)), out_dtype):
+        best = None
+        for sub in _subtrees(expr, []):
+            ids = _leaf_ids(sub)
+            if _fits(sub, len(ids), _etype(sub)) and (best is None or _size(sub) > _size(best)):
+                best = sub
+        if best is None:  # cannot happen: an operator over two leaves always fits
+            raise NotImplementedError("expression cannot be split into device programs")
+        piece = CuProcView(leaves, best, _etype(best), shape)._prune()
+        tmp = CuNArray.empty(shape, piece.dtype)
+        prog, raises = compile_program(piece._expr, piece.dtype)
+        can_raise = can_raise or raises
+        ins = (A.View * max(1, len(piece._leaves)))()
+        for k, l in enumerate(piece._leaves):
+            ins[k] = l._cview()
+        A.check(lib().phcu_eval(ctypes.byref(prog), ins, len(piece._leaves), ctypes.byref(tmp._view())),
+                "phcu_eval")
+        temps.append(tmp)
+        leaves = leaves + [tmp._as_leaf()]
+        expr = _replace(expr, best, ("in", len(leaves) - 1, piece.dtype))
+        used = sorted(_leaf_ids(expr))
+        remap = {old: new for new, old in enumerate(used)}
+        expr = _remap(expr, remap)
+        leaves = [leaves[i] for i in used]
+    return expr, leaves, temps, can_raise
+
+
+def _leaf_ids(e, acc=None):
+    acc = set() if acc is None else acc
+    k = e[0]
+    if k == "in":
+        acc.add(e[1])
+    elif k == "bin":
+        _leaf_ids(e[2], acc)
+        _leaf_ids(e[3], acc)
+    elif k in ("un", "cvt"):
+        _leaf_ids(e[2], acc)
+    return acc
 
 
 def _remap(e, m):

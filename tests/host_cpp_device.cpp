@@ -106,10 +106,10 @@ static void run_proc(const std::string& tag) {
   D.set_chunk({rng(1, -1)}, D.view({rng(0, -2)}).process() * 2);  // reads the rows it writes
   save(tag + "_proc_overlap", D.to_vector());
   save(tag + "_proc_const", A.process([](auto) { return 2.5f; }).to_vector());
-  // five distinct operand views: A, B, A reversed on axis 1, B reversed on
-  // axis 1, A reversed on every axis (CuView - CuView alone would be eager)
-  expect_raise(tag + "_proc_five",
-               [&] { return ((A.process() + B) * (A.view(rev).process() - B.view(rev)) + A.reverse()).to_cu(); });
+  // five distinct operand views (A, B, A and B reversed on axis 1, A reversed
+  // on every axis; CuView - CuView alone would be eager): more than one device
+  // program reads, so the expression runs as two programs
+  save(tag + "_proc_five", ((A.process() + B) * (A.view(rev).process() - B.view(rev)) + A.reverse()).to_vector());
 }
 
 static void run_proc_mixed() {

@@ -183,7 +183,11 @@ def test_fused_chains(run_proc, ora, tag):
     d[1:] = ora.map_binary_scalar(ora.OP_MUL, np.ascontiguousarray(a[:-1]), 2, t)[0]
     assert np.array_equal(load(tag + "_proc_overlap", dt), d.reshape(-1))
     assert np.all(load(tag + "_proc_const", np.float32) == np.float32(2.5))
-    assert "raised %s_proc_five NotImplementedError" % tag in lines  # five operand views
+    # five operand views: split into two device programs, same results
+    five, _ = ora.map_binary(ora.OP_ADD, a, b)
+    five, _ = ora.map_binary(ora.OP_MUL, five, ora.map_binary(ora.OP_SUB, rev(a), rev(b))[0])
+    five, _ = ora.map_binary(ora.OP_ADD, five, np.ascontiguousarray(a[::-1, ::-1, ::-1]))
+    assert np.array_equal(load(tag + "_proc_five", dt), five.reshape(-1))
 
 
 def test_fused_mixed_types_and_checked_int32(run_proc, ora):
