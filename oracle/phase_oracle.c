@@ -492,6 +492,24 @@ static void parallel_for(int64_t n, int nthreads, void (*fn)(void*, int64_t, int
   for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
 }
 
+/* parallel_for over the piece [lo, hi) of an index range */
+typedef struct {
+  void (*fn)(void*, int64_t, int64_t);
+  void* arg;
+  int64_t base;
+} offset_arg_t;
+
+static void offset_piece(void* p, int64_t lo, int64_t hi) {
+  offset_arg_t* o = (offset_arg_t*)p;
+  o->fn(o->arg, o->base + lo, o->base + hi);
+}
+
+static void parallel_for_range(int64_t lo, int64_t hi, int nthreads, void (*fn)(void*, int64_t, int64_t),
+                               void* arg) {
+  offset_arg_t o = {fn, arg, lo};
+  parallel_for(hi - lo, nthreads, offset_piece, &o);
+}
+
 /* ================================================================= gather */
 
 typedef struct {
@@ -518,6 +536,17 @@ int ora_gather(const ora_operand_t* a, void* out, int nthreads) {
   int64_t n = shape_size(a->shape, a->rank);
   gather_arg_t g = {a, (char*)out};
   parallel_for(n, nthreads, gather_piece, &g);
+  return ORA_OK;
+}
+
+/* The elements [lo, hi) (lexicographic positions) of ora_gather's output,
+ * written at their positions in `out`: a slab of the same operation for a
+ * bounded timing sample. */
+int ora_gather_range(const ora_operand_t* a, void* out, int64_t lo, int64_t hi, int nthreads) {
+  int64_t n = shape_size(a->shape, a->rank);
+  if (lo < 0 || hi > n || lo > hi) return ORA_ERR_INDEX;
+  gather_arg_t g = {a, (char*)out};
+  parallel_for_range(lo, hi, nthreads, gather_piece, &g);
   return ORA_OK;
 }
 
@@ -664,6 +693,41 @@ int ora_scatter(const ora_operand_t* dst, const ora_operand_t* src) {
     lex_advance(sc, src->shape, src->rank);
     lex_advance(dc, dst->shape, dst->rank);
   }
+  return ORA_OK;
+}
+
+/* The writes [lo, hi) of ora_scatter, split over threads: only for a source
+ * that does not alias the destination (element order is then irrelevant);
+ * a slab of the same operation for a bounded timing sample. */
+typedef struct {
+  const ora_operand_t *dst, *src;
+} scatter_arg_t;
+
+static void scatter_piece(void* p, int64_t lo, int64_t hi) {
+  scatter_arg_t* a = (scatter_arg_t*)p;
+  opctx_t cd, cs;
+  opctx_init(&cd, a->dst);
+  opctx_init(&cs, a->src);
+  int64_t dc[ORA_MAX_RANK], sc[ORA_MAX_RANK];
+  index_to_coord(lo, a->dst->shape, a->dst->rank, dc);
+  index_to_coord(lo, a->src->shape, a->src->rank, sc);
+  char* d = (char*)a->dst->buf;
+  const char* s = (const char*)a->src->buf;
+  for (int64_t i = lo; i < hi; i++) {
+    memcpy(d + opctx_index(&cd, dc) * cd.es, s + opctx_index(&cs, sc) * cs.es, cd.es);
+    lex_advance(sc, a->src->shape, a->src->rank);
+    lex_advance(dc, a->dst->shape, a->dst->rank);
+  }
+}
+
+int ora_scatter_range(const ora_operand_t* dst, const ora_operand_t* src, int64_t lo, int64_t hi, int nthreads) {
+  int64_t n = shape_size(dst->shape, dst->rank);
+  if (!ora_compatible_shapes(src->shape, src->rank, dst->shape, dst->rank)) return ORA_ERR_SHAPE;
+  if (n != shape_size(src->shape, src->rank)) return ORA_ERR_SHAPE;
+  if (ora_dtype_size(dst->dtype) != ora_dtype_size(src->dtype)) return ORA_ERR_UNSUPPORTED;
+  if (lo < 0 || hi > n || lo > hi) return ORA_ERR_INDEX;
+  scatter_arg_t a = {dst, src};
+  parallel_for_range(lo, hi, nthreads, scatter_piece, &a);
   return ORA_OK;
 }
 
@@ -1026,6 +1090,26 @@ int ora_map_binary(int op, const ora_operand_t* a, const ora_operand_t* b, void*
   m.op = op; m.a = a; m.b = b; m.tout = tout; m.out = (char*)out;
   pthread_mutex_init(&m.mu, NULL);
   parallel_for(shape_size(a->shape, a->rank), nthreads, map_piece, &m);
+  pthread_mutex_destroy(&m.mu);
+  *status = m.status;
+  return ORA_OK;
+}
+
+/* The elements [lo, hi) of ora_map_binary's output (a timing slab). */
+int ora_map_binary_range(int op, const ora_operand_t* a, const ora_operand_t* b, void* out, int64_t lo, int64_t hi,
+                         uint32_t* status, int nthreads) {
+  if (a->rank != b->rank) return ORA_ERR_SHAPE;
+  for (int i = 0; i < a->rank; i++)
+    if (a->shape[i] != b->shape[i]) return ORA_ERR_SHAPE;
+  if (lo < 0 || hi > shape_size(a->shape, a->rank) || lo > hi) return ORA_ERR_INDEX;
+  int tout;
+  int rc = ora_result_dtype(op, a->dtype, b->dtype, &tout);
+  if (rc) return rc;
+  map_arg_t m;
+  memset(&m, 0, sizeof(m));
+  m.op = op; m.a = a; m.b = b; m.tout = tout; m.out = (char*)out;
+  pthread_mutex_init(&m.mu, NULL);
+  parallel_for_range(lo, hi, nthreads, map_piece, &m);
   pthread_mutex_destroy(&m.mu);
   *status = m.status;
   return ORA_OK;

@@ -157,6 +157,13 @@ int ora_dtype_size(int dtype);
 
 /* View#to_narr / get_chunk on a view: lexicographic gather (view.cr:123-126). */
 int ora_gather(const ora_operand_t* a, void* out, int nthreads);
+/* Slabs [lo, hi) of the lexicographic output of gather / map_binary / scatter,
+ * each element at its own position (bounded timing samples of a full-size
+ * operation; ora_scatter_range requires a source that does not alias dst). */
+int ora_gather_range(const ora_operand_t* a, void* out, int64_t lo, int64_t hi, int nthreads);
+int ora_map_binary_range(int op, const ora_operand_t* a, const ora_operand_t* b, void* out, int64_t lo, int64_t hi,
+                         uint32_t* status, int nthreads);
+int ora_scatter_range(const ora_operand_t* dst, const ora_operand_t* src, int64_t lo, int64_t hi, int nthreads);
 /* NArray#unsafe_fetch_chunk with the buffer-index odometer (n_array.cr:450-453). */
 int ora_narray_fetch_chunk(const void* buf, int dtype, const int64_t* shape, int rank,
                            const ora_region_t* region, void* out, int nthreads);

@@ -17,7 +17,8 @@ BUILDDIR = os.path.join(HERE, "_build")
 LIBNAME = "libphcuda.so"
 
 SOURCES = ["runtime.cu", "plan.cu", "eval.cu", "eval_inst_u32_lo.cu", "eval_inst_u32_hi.cu", "eval_inst_u64_lo.cu",
-           "eval_inst_u64_hi.cu", "reduce.cu", "stencil.cu", "batch.cu", "tuner.cu"]
+           "eval_inst_u64_hi.cu", "reduce.cu", "stencil.cu", "batch.cu", "batch_k32n2.cu", "batch_k32n4.cu",
+           "batch_k64.cu", "tuner.cu"]
 
 # -fmad=false: no FMA contraction anywhere, so single Float32 operations round
 # exactly as on the host; IEEE division and square root stay the default.

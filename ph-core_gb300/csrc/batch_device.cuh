@@ -1,0 +1,270 @@
+// batch_device.cuh -- work items, bodies and the persistent kernel of the
+// batched executor (batch.cu holds the host side).  Each instantiation of
+// batch_kernel lives in its own translation unit (batch_k*.cu), so they
+// compile in parallel.
+//
+// The bodies are those of the standalone kernels: ROW and TILE with the
+// reduced interpreter for pre-decoded programs (copies and single operators
+// included) or the general one otherwise, and the element-load reduction
+// bodies (GROUP with the planner's lanes per output, or COLUMN).  Each is a
+// separate (not inlined) function, so every body gets its own register
+// allocation instead of the sum of all of them.
+#pragma once
+
+#include "eval_device.cuh"
+#include "reduce_device.cuh"
+
+namespace phcu {
+
+enum BKind : int32_t { BK_ROW = 0, BK_TILE = 1, BK_REDUCE = 2 };
+
+// What a block needs to run one task's items (staged in shared memory).
+struct BHead {
+  int32_t kind;
+  int32_t fast;     // ROW / TILE: FAST_FX (pre-decoded program) or FAST_NONE
+  int32_t vec;      // ROW: elements per chunk (1 or 4)
+  int32_t rmode;    // REDUCE: 0 GROUP, 1 COLUMN
+  int32_t rG;       // REDUCE GROUP: lanes per output
+  int32_t counter;  // REDUCE split over several items: arrival counter, else -1
+  int64_t item0, nitems, per_item, nunits;
+};
+
+struct BTask {
+  BHead h;
+  int32_t prog;
+  int32_t pad;
+  int64_t bytes;
+  int64_t order_key;
+  EvalPlan ep;
+  RedArgs ra;
+};
+
+constexpr int BATCH_THREADS = 256;
+constexpr int BATCH_MIN_BLOCKS = 3;
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// ------------------------------------------------------------ ROW bodies
+// Chunks [u0, u1) of VEC elements; a thread takes U chunks blockDim apart per pass.
+template <typename S, int NIN, int VEC, int U, bool STASH, int FAST>
+__device__ __forceinline__ void row_item(const EvalPlan& p, const phcu_program_t& prog, int64_t u0, int64_t u1,
+                                         uint32_t& st) {
+  const uint32_t step = blockDim.x;
+  for (int64_t c = u0 + threadIdx.x; c < u1; c += (int64_t)step * U)
+    row_group<S, NIN, VEC, U, STASH, FAST>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
+}
+
+// Elements per thread per pass (as the standalone ROW kernels): pre-decoded
+// programs 8 with 32-bit slots (4 with 64-bit slots), the general
+// interpreter 4; single-element chunks take half as many.
+template <typename S, int FAST>
+constexpr int batch_v() {
+  return (sizeof(S) == 8 || FAST == FAST_NONE) ? 4 : 8;
+}
+
+template <typename S, int NIN, int FAST>
+__device__ __forceinline__ void row_fast(const BHead& h, const EvalPlan& p, const phcu_program_t& prog, int64_t u0,
+                                         int64_t u1, uint32_t& st) {
+  constexpr int V = batch_v<S, FAST>();
+  constexpr bool STASH = FAST == FAST_NONE;
+  if (h.vec == 4) row_item<S, NIN, 4, V / 4, STASH, FAST>(p, prog, u0, u1, st);
+  else row_item<S, NIN, 1, V / 2, STASH, FAST>(p, prog, u0, u1, st);
+}
+
+template <typename S, int NIN>
+__device__ __noinline__ void run_row(const BHead& h, const EvalPlan& p, const phcu_program_t& prog, int64_t u0,
+                                     int64_t u1, uint32_t& st) {
+  if (h.fast == FAST_FX) row_fast<S, NIN, FAST_FX>(h, p, prog, u0, u1, st);
+  else row_fast<S, NIN, FAST_NONE>(h, p, prog, u0, u1, st);
+}
+
+// ----------------------------------------------------------- TILE bodies
+template <typename S, int NIN>
+__device__ __noinline__ void run_tile(const BHead& h, const EvalPlan& p, const phcu_program_t& prog, int64_t u0,
+                                      int64_t u1, S* tiles, uint32_t& st) {
+  if (h.fast == FAST_FX) {
+    for (int64_t t = u0; t < u1; t++) tile_body<S, NIN, false, FAST_FX>(p, prog, (uint64_t)t, tiles, st);
+  } else {
+    for (int64_t t = u0; t < u1; t++) tile_body<S, NIN, true, FAST_NONE>(p, prog, (uint64_t)t, tiles, st);
+  }
+}
+
+// ------------------------------------------------------ REDUCE bodies
+// Units [u0, u1) are (output, split) pairs; GROUP (G lanes per unit) or
+// COLUMN (one thread per unit), element loads.
+template <typename T, int KIND>
+__device__ __forceinline__ void red_units(const BHead& h, const RedArgs& a, int64_t u0, int64_t u1, uint32_t& st) {
+  if (h.rmode == 1) {
+    for (int64_t w = u0 + threadIdx.x; w < u1; w += blockDim.x) column_one<T, KIND>(a, w % a.O, w / a.O, st);
+    return;
+  }
+  const int G = h.rG;
+  const int lane = threadIdx.x & 31;
+  const int glane = lane & (G - 1);
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+  const int groups = blockDim.x / G;
+  for (int64_t w = u0 + threadIdx.x / G; w < u1; w += groups)
+    group_one_g<T, KIND>(a, w % a.O, w / a.O, G, glane, gmask, st);
+}
+
+template <typename T, int KIND>
+__device__ __forceinline__ void red_combine(const RedArgs& a, CombineScratch& cs, uint32_t& st) {
+  if (a.S >= 32) {
+    for (int64_t o = 0; o < a.O; o++) combine_block<T, KIND>(a, o, cs, st);  // uniform loop: all threads
+  } else {
+    for (int64_t o = threadIdx.x; o < a.O; o += blockDim.x) combine_one<T, KIND>(a, o, st);
+  }
+}
+
+template <bool WIDE>
+__device__ __noinline__ void run_reduce(const BHead& h, const RedArgs& a, int64_t u0, int64_t u1, uint32_t& st) {
+  const bool sum = a.op == PHCU_RED_SUM;
+  switch (a.dtype) {
+    case PHCU_F32:
+      if (sum) red_units<float, RK_SUM>(h, a, u0, u1, st);
+      else red_units<float, RK_EXT>(h, a, u0, u1, st);
+      break;
+    case PHCU_I32:
+      if (sum) red_units<int32_t, RK_SUM>(h, a, u0, u1, st);
+      else red_units<int32_t, RK_EXT>(h, a, u0, u1, st);
+      break;
+    case PHCU_F64:
+      if constexpr (WIDE) {
+        if (sum) red_units<double, RK_SUM>(h, a, u0, u1, st);
+        else red_units<double, RK_EXT>(h, a, u0, u1, st);
+      }
+      break;
+    default:
+      if constexpr (WIDE) {
+        if (sum) red_units<long long, RK_SUM>(h, a, u0, u1, st);
+        else red_units<long long, RK_EXT>(h, a, u0, u1, st);
+      }
+  }
+}
+
+template <bool WIDE>
+__device__ __noinline__ void run_combine(const RedArgs& a, CombineScratch& cs, uint32_t& st) {
+  const bool sum = a.op == PHCU_RED_SUM;
+  switch (a.dtype) {
+    case PHCU_F32:
+      if (sum) red_combine<float, RK_SUM>(a, cs, st);
+      else red_combine<float, RK_EXT>(a, cs, st);
+      break;
+    case PHCU_I32:
+      if (sum) red_combine<int32_t, RK_SUM>(a, cs, st);
+      else red_combine<int32_t, RK_EXT>(a, cs, st);
+      break;
+    case PHCU_F64:
+      if constexpr (WIDE) {
+        if (sum) red_combine<double, RK_SUM>(a, cs, st);
+        else red_combine<double, RK_EXT>(a, cs, st);
+      }
+      break;
+    default:
+      if constexpr (WIDE) {
+        if (sum) red_combine<long long, RK_SUM>(a, cs, st);
+        else red_combine<long long, RK_EXT>(a, cs, st);
+      }
+  }
+}
+
+struct BatchArgs {
+  const BTask* tasks;
+  const int32_t* item_task;
+  const phcu_program_t* progs;
+  unsigned long long* ticket;
+  uint32_t* counters;
+  uint32_t* status;
+  int64_t n_items;
+  uint64_t deadline_ns;  // global-timer budget per launch
+};
+
+constexpr size_t PLAN_BYTES = sizeof(EvalPlan) > sizeof(RedArgs) ? sizeof(EvalPlan) : sizeof(RedArgs);
+
+// S: program slot width; NIN: inputs per program (2 or 4); WIDE: reductions
+// of 64-bit elements.  Blocks take items with an atomic ticket until the list
+// (or the global-timer deadline) runs out; a task's plan and program are
+// copied into shared memory when the block's task changes.
+template <typename S, int NIN, bool WIDE>
+__global__ void __launch_bounds__(BATCH_THREADS, BATCH_MIN_BLOCKS) batch_kernel(const __grid_constant__ BatchArgs A) {
+  extern __shared__ __align__(16) unsigned char tiles_raw[];
+  S* tiles = reinterpret_cast<S*>(tiles_raw);
+  __shared__ __align__(16) unsigned char s_plan[PLAN_BYTES];
+  __shared__ __align__(16) phcu_program_t s_prog;
+  __shared__ BHead s_head;
+  __shared__ long long s_item;
+  __shared__ int s_flag;
+  __shared__ CombineScratch s_combine;
+  uint32_t st = 0;
+  int cur = -1;  // task whose plan is in shared memory
+  const uint64_t t_start = global_ns();
+  for (;;) {
+    if (threadIdx.x == 0) {
+      long long it = (long long)atomicAdd(A.ticket, 1ull);
+      if (global_ns() - t_start > A.deadline_ns) {
+        st |= PHCU_ST_TIMEOUT;
+        it = A.n_items;  // give up: the host sees TIMEOUT in the status word
+      }
+      s_item = it;
+    }
+    __syncthreads();
+    const long long item = s_item;
+    if (item >= A.n_items) break;
+    const int ti = A.item_task[item];
+    if (ti != cur) {  // uniform: every thread read the same item
+      const BTask& T = A.tasks[ti];
+      const bool red = T.h.kind == BK_REDUCE;
+      const uint32_t* src = red ? (const uint32_t*)&T.ra : (const uint32_t*)&T.ep;
+      const int words = (int)((red ? sizeof(RedArgs) : sizeof(EvalPlan)) / 4);
+      for (int i = threadIdx.x; i < words; i += blockDim.x) ((uint32_t*)s_plan)[i] = src[i];
+      if (!red) {
+        const uint32_t* ps = (const uint32_t*)&A.progs[T.prog];
+        for (int i = threadIdx.x; i < (int)(sizeof(phcu_program_t) / 4); i += blockDim.x)
+          ((uint32_t*)&s_prog)[i] = ps[i];
+      }
+      if (threadIdx.x == 0) s_head = T.h;
+      cur = ti;
+      __syncthreads();
+    }
+    const BHead& h = s_head;
+    const int64_t local = item - h.item0;
+    const int64_t u0 = local * h.per_item;
+    const int64_t u1 = min(h.nunits, u0 + h.per_item);
+    if (h.kind == BK_ROW) {
+      run_row<S, NIN>(h, *reinterpret_cast<const EvalPlan*>(s_plan), s_prog, u0, u1, st);
+    } else if (h.kind == BK_TILE) {
+      run_tile<S, NIN>(h, *reinterpret_cast<const EvalPlan*>(s_plan), s_prog, u0, u1, tiles, st);
+    } else {
+      const RedArgs& a = *reinterpret_cast<const RedArgs*>(s_plan);
+      run_reduce<WIDE>(h, a, u0, u1, st);
+      if (h.counter >= 0) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          __threadfence();
+          const uint32_t arrived = atomicAdd(&A.counters[h.counter], 1u);
+          s_flag = (arrived == (uint32_t)(h.nitems - 1));
+        }
+        __syncthreads();
+        if (s_flag) {
+          __threadfence();
+          run_combine<WIDE>(a, s_combine, st);
+        }
+      }
+    }
+    __syncthreads();  // s_item (and, for a new task, the staged plan) is rewritten next
+  }
+  if (st) atomicOr(A.status, st);
+}
+
+using BatchKernel = void (*)(BatchArgs);
+
+// The instantiations (batch_k32n2.cu, batch_k32n4.cu, batch_k64.cu).
+BatchKernel batch_kernel_u32_nin2();
+BatchKernel batch_kernel_u32_nin4();
+BatchKernel batch_kernel_u64();
+
+}  // namespace phcu

@@ -189,11 +189,11 @@ static int32_t launch_reduce(const RedArgs& a, const RedShape& sh) {
 }
 
 // Launches an already planned reduction (used by the batched executor's per-op replay).
-int32_t launch_reduce_plan(const RedArgs& a, int mode, int G) {
+int32_t launch_reduce_plan(const RedArgs& a, int mode, int G, int vec) {
   RedShape sh;
   sh.mode = mode;
   sh.G = G;
-  sh.vec = 0;  // the batched executor's plans replay with element loads
+  sh.vec = vec;
   return launch_reduce(a, sh);
 }
 

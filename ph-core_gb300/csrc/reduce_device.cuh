@@ -293,9 +293,9 @@ __device__ __forceinline__ void finish(const RedArgs& a, int64_t o, int64_t spli
 // ------------------------------------------------------ per-output bodies
 // GROUP: the G lanes of one group reduce elements [k0, k1) of output o; lane 0
 // of the group finishes (or stores the partial of split `split`).
-template <typename T, int KIND, int G>
-__device__ __forceinline__ void group_one(const RedArgs& a, int64_t o, int64_t split, int glane, unsigned gmask,
-                                          uint32_t& st) {
+template <typename T, int KIND>
+__device__ __forceinline__ void group_one_g(const RedArgs& a, int64_t o, int64_t split, const int G, int glane,
+                                            unsigned gmask, uint32_t& st) {
   const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
   const int64_t k0 = split * a.chunk;
   const int64_t k1 = min(a.K, k0 + a.chunk);
@@ -328,6 +328,13 @@ __device__ __forceinline__ void group_one(const RedArgs& a, int64_t o, int64_t s
     else eacc.shfl(d, gmask, G, is_max);
   }
   if (glane == 0) finish<T, KIND>(a, o, split, sacc, eacc, st);
+}
+
+// group_one_g with a compile-time group size (the standalone kernels).
+template <typename T, int KIND, int G>
+__device__ __forceinline__ void group_one(const RedArgs& a, int64_t o, int64_t split, int glane, unsigned gmask,
+                                          uint32_t& st) {
+  group_one_g<T, KIND>(a, o, split, G, glane, gmask, st);
 }
 
 // GROUP over NO outputs at once (short contiguous axes): each lane keeps NO
