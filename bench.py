@@ -33,7 +33,12 @@ SHAPE = [512, 512, 256]
 METRIC = "HBM GB/s vs ~8 TB/s peak; batched ops/s fused vs per-op launches, same GPU"
 WORKLOAD = ("large strided views: Float32+Int32 512x512x256, permute(2,0,1) and reversed-axis-1 views, "
             "+ - * / on both view kinds, MutableView scatter")
-CPU_SAMPLE_SHAPE = [128, 128, 64]
+
+
+def bench_config():
+    """The workload both arms measure (the device arm and --impl reference)."""
+    return {"workload": WORKLOAD, "shape": SHAPE, "dtypes": ["Float32", "Int32"],
+            "l2": "inputs larger than L2 (256 MiB operands), no flush", "parallelism": "replicas"}
 
 
 def peaks():
@@ -138,7 +143,7 @@ def device_arm(args):
     return _device_timed(args, cu, A, lib, arrays, dev, jobs, run_job, step_bytes)
 
 
-def make_jobs(cu, A, dev, n):
+def make_jobs(cu, A, dev, n, shape=SHAPE):
     """Descriptors of every operation of one step (outputs preallocated).
     dev maps dtype tag -> (A, B, C) device arrays."""
     if True:
@@ -150,10 +155,11 @@ def make_jobs(cu, A, dev, n):
             bp = B_.view().permute(2, 0, 1)
             ar = A_.view(slice(None), cu.R(None, None, -1), slice(None))
             br = B_.view(slice(None), cu.R(None, None, -1), slice(None))
-            out_p = cu.CuNArray.empty([256, 512, 512], A_.dtype)
-            out_r = cu.CuNArray.empty(SHAPE, A_.dtype)
-            out64_p = cu.CuNArray.empty([256, 512, 512], cu.Float64)
-            out64_r = cu.CuNArray.empty(SHAPE, cu.Float64)
+            pshape = [shape[2], shape[0], shape[1]]
+            out_p = cu.CuNArray.empty(pshape, A_.dtype)
+            out_r = cu.CuNArray.empty(shape, A_.dtype)
+            out64_p = cu.CuNArray.empty(pshape, cu.Float64)
+            out64_r = cu.CuNArray.empty(shape, cu.Float64)
             jobs.append(("gather_permute", "copy", (out_p._view(), ap._cview()), 2 * n * es, [out_p]))
             jobs.append(("gather_reverse", "copy", (out_r._view(), ar._cview()), 2 * n * es, [out_r]))
             ops = [A.OP_ADD, A.OP_SUB, A.OP_MUL if dt == "f32" else A.OP_WMUL, A.OP_DIV]
@@ -188,16 +194,17 @@ def profile_class(args):
 
     cu.init(0)
     lib = A.load()
-    n = int(np.prod(SHAPE))
+    shape = [int(x) for x in args.profile_shape.split("x")] if args.profile_shape else SHAPE
+    n = int(np.prod(shape))
     dt = args.profile_dtype
     if dt == "f32":
-        a, b = synth.uniform_f32(SHAPE, seed=0), synth.uniform_f32(SHAPE, seed=0, start=n)
+        a, b = synth.uniform_f32(shape, seed=0), synth.uniform_f32(shape, seed=0, start=n)
     else:
-        a = synth.uniform_i32(SHAPE, seed=0, lo=-2 ** 20, hi=2 ** 20)
-        b = synth.uniform_i32(SHAPE, seed=0, lo=-2 ** 20, hi=2 ** 20, start=n)
+        a = synth.uniform_i32(shape, seed=0, lo=-2 ** 20, hi=2 ** 20)
+        b = synth.uniform_i32(shape, seed=0, lo=-2 ** 20, hi=2 ** 20, start=n)
     Ad, Bd = cu.CuNArray.from_numpy(a), cu.CuNArray.from_numpy(b)
-    dev = {dt: (Ad, Bd, cu.CuNArray.empty([256, 512, 512], Ad.dtype))}
-    jobs = [j for j in make_jobs(cu, A, dev, n) if j[0] == args.profile_class]
+    dev = {dt: (Ad, Bd, cu.CuNArray.empty([shape[2], shape[0], shape[1]], Ad.dtype))}
+    jobs = [j for j in make_jobs(cu, A, dev, n, shape) if j[0] == args.profile_class]
     for _ in range(args.warmup):
         for j in jobs:
             execute_job(lib, A, j)
@@ -240,8 +247,9 @@ def measured_traffic(cls):
 
 def profile_config(args):
     """One untimed pass of a secondary workload, for ncu: c3 (the fused chain
-    over 64x128x128x64, then sum/max/argmax along every axis and the full sum)
-    or c4 (8 heat steps on 4096x4096 without a graph)."""
+    over 64x128x128x64, then sum/max/argmax along every axis and the full sum),
+    c4 (8 heat steps on 4096x4096 without a graph) or c5 (the 10,000-task
+    uneven batch: two persistent launches)."""
     import phase_cu as cu
     from phase_cu import _abi as A
     from phase_cu import synth
@@ -255,6 +263,15 @@ def profile_config(args):
         for k in range(4):
             r.sum(axis=k), r.max(axis=k), r.argmax(axis=k)
         r.sum()
+    elif args.profile_config == "c5":
+        from phase_cu.batch import Batch, Workload
+
+        wl = Workload(n_tasks=10000, seed=0)
+        b = Batch(wl.tasks(), wl.programs)
+        b.launch(0)
+        b.launch(0)
+        A.call("phcu_sync")
+        b.close()
     else:
         from phase_cu import stencil
 
@@ -366,9 +383,9 @@ def _device_timed(args, cu, A, lib, arrays, dev, jobs, run_job, step_bytes):
         "metric": METRIC, "value": round(value, 1), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32", "data": "synthetic (SplitMix64, seed 0)",
-        "config": {"workload": WORKLOAD, "shape": SHAPE, "bytes_per_step": step_bytes,
-                   "execution": "step captured once as a CUDA graph, one graph launch per step",
-                   "l2": "inputs larger than L2 (256 MiB operands), no flush", "parallelism": "replicas"},
+        "config": bench_config(),
+        "execution": "step captured once as a CUDA graph, one graph launch per step; %d algorithmic bytes per step"
+                     % step_bytes,
         "gpu_launches": launches_per_step * args.steps, "roofline": roofline, "clocks": clk, "e2e": e2e,
         "direct_calls": {"ms_per_step": round(direct_ms, 4),
                          "value": round(job_gbs(step_bytes, 1, direct_ms), 1),
@@ -452,6 +469,7 @@ def e2e_leg(A, lib, arrays, dev_arrays, jobs, args, timer, stop, step_bytes):
     t = timer()
     run_steps(dev_arrays, steps)
     ms = stop(t) / steps
+    check = e2e_check(A, lib, arrays, own, upload, dev_arrays)
     h2d = sum(2 * v[2] for v in host_in.values())
     d2h = sum(x[2]._buf.nbytes for x in own)
     for v in host_in.values():
@@ -462,7 +480,62 @@ def e2e_leg(A, lib, arrays, dev_arrays, jobs, args, timer, stop, step_bytes):
     return {"value": round(step_bytes / (ms * 1e-3) / 1e9, 1), "unit": "GB/s", "ms_per_step": round(ms, 3),
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": steps,
             "path": ("phcu_upload_async/phcu_copy/phcu_binary/phcu_download_async/phcu_transfer_wait "
-                     "on pinned host buffers")}
+                     "on pinned host buffers"), "check": check}
+
+
+def expected_results(arrays):
+    """The step's results computed on the host with numpy, in the order of
+    make_jobs (IEEE single operations, Int32 wrapping multiply, Int32 / Int32
+    as Float64 division): an independent check of what the e2e leg downloads."""
+    for dt, (a, b) in arrays.items():
+        ap, bp = np.transpose(a, (2, 0, 1)), np.transpose(b, (2, 0, 1))
+        ar, br = a[:, ::-1, :], b[:, ::-1, :]
+        yield np.ascontiguousarray(ap)
+        yield np.ascontiguousarray(ar)
+        for x, y in ((ap, bp), (ar, br)):
+            with np.errstate(all="ignore"):
+                yield x + y
+                yield x - y
+                yield x * y
+                yield (x.astype(np.float64) / y.astype(np.float64)) if dt == "i32" else x / y
+        c = np.empty([256, 512, 512], dtype=a.dtype)
+        c[:, ::-1, :] = ap
+        yield c
+
+
+def e2e_check(A, lib, arrays, own, upload, dev_arrays):
+    """After the timed steps: (1) the last two pinned staging buffers (the last
+    two results of the last timed step) equal the device results; (2) one more
+    step through the same upload / operation / async download path, each
+    download compared with the numpy result of that operation."""
+    def host_view(ptr, nbytes, dtype):
+        raw = (ctypes.c_uint8 * nbytes).from_address(ptr)
+        return np.frombuffer(raw, dtype=np.uint8).view(dtype)
+
+    def device_bytes(t):
+        h = np.empty(t._buf.nbytes, dtype=np.uint8)
+        A.check(lib.phcu_download(h.ctypes.data, t._buf.ptr, t._buf.nbytes))
+        return h
+
+    last_ok = True
+    for i in (len(own) - 2, len(own) - 1):
+        t, hbuf = own[i][2], own[i][3]
+        last_ok = last_ok and bool(np.array_equal(host_view(hbuf, t._buf.nbytes, np.uint8), device_bytes(t)))
+    upload(dev_arrays)
+    A.check(lib.phcu_transfer_wait())
+    bad = []
+    for i, ((kind, a, target, hbuf, _), exp) in enumerate(zip(own, expected_results(arrays))):
+        if kind == "copy":
+            A.check(lib.phcu_copy(ctypes.byref(a[0]), ctypes.byref(a[1])))
+        else:
+            A.check(lib.phcu_binary(a[0], ctypes.byref(a[1]), ctypes.byref(a[2]), ctypes.byref(a[3])))
+        A.check(lib.phcu_download_async(hbuf, target._buf.ptr, target._buf.nbytes))
+        A.check(lib.phcu_transfer_wait())
+        got = host_view(hbuf, target._buf.nbytes, exp.dtype).reshape(exp.shape)
+        if not np.array_equal(got, exp, equal_nan=exp.dtype.kind == "f"):
+            bad.append(i)
+    return {"results_checked": len(own), "mismatches": bad, "last_timed_step_equals_device": last_ok,
+            "reference": "numpy on the host inputs (IEEE single ops, wrapping Int32 *, Float64 division)"}
 
 
 # --------------------------------------------------------- other configs
@@ -481,6 +554,44 @@ def _ms(A, lib, fn, reps, flush=False):
     return statistics.median(out)
 
 
+C1_REPS = 50
+
+
+def _flushed_graph_ms(A, lib, fn, reps=C1_REPS):
+    """Device time of fn() with a cold L2: a CUDA graph of `reps` (L2 flush,
+    fn) pairs and one of `reps` flushes alone are each replayed five times;
+    the difference of the median replay times over reps."""
+    A.check(lib.phcu_l2_flush())  # allocates the scrub buffer before any capture
+    fn()
+    A.call("phcu_sync")
+
+    def graph(with_op):
+        g = ctypes.c_void_p()
+        A.check(lib.phcu_graph_begin())
+        for _ in range(reps):
+            A.check(lib.phcu_l2_flush())
+            if with_op:
+                fn()
+        A.check(lib.phcu_graph_end(ctypes.byref(g)))
+        return g
+
+    g_op, g_fl = graph(True), graph(False)
+    t_op, t_fl = [], []
+    for _ in range(5):
+        t_op.append(_ms(A, lib, lambda: A.check(lib.phcu_graph_launch(g_op)), 1))
+        t_fl.append(_ms(A, lib, lambda: A.check(lib.phcu_graph_launch(g_fl)), 1))
+    lib.phcu_graph_destroy(g_op)
+    lib.phcu_graph_destroy(g_fl)
+    return max(1e-6, (statistics.median(t_op) - statistics.median(t_fl)) / reps)
+
+
+def _ms_batched(A, lib, fn, reps=5, inner=10):
+    """Median over reps of the mean device time of `inner` back-to-back calls
+    (one event pair around them): the per-launch event and gap overhead is
+    spread over `inner` launches.  For kernels whose inputs exceed L2."""
+    return _ms(A, lib, lambda: [fn() for _ in range(inner)], reps) / inner
+
+
 def extra_configs(reps=5):
     """The remaining workloads, each measured on its own (GB/s = algorithmic
     bytes / median device time)."""
@@ -492,7 +603,10 @@ def extra_configs(reps=5):
     res = {}
     gb = lambda nbytes, ms: round(nbytes / (ms * 1e-3) / 1e9, 1)
 
-    # C1: 1024x1024 a+b, a*b, a[.., 1..2..-1]; 12 MiB fits L2, so L2 is flushed before each rep
+    # C1: 1024x1024 a+b, a*b, a[.., 1..2..-1]; 12 MiB fits L2, so L2 is flushed before each rep.
+    # One event pair around one such launch reads the launch and event overhead
+    # (~9 us for any of these ops), so each op is timed as a CUDA graph of
+    # C1_REPS (flush, op) pairs minus a graph of C1_REPS flushes alone.
     c1 = {}
     n = 1024 * 1024
     for dt in ("f32", "i32"):
@@ -506,11 +620,13 @@ def extra_configs(reps=5):
         sv = X.view(slice(None), cu.R(1, -1, 2))._cview()
         gv = G._view()
         for name, op in (("add", A.OP_ADD), ("mul", A.OP_MUL if dt == "f32" else A.OP_WMUL)):
-            ms = _ms(A, lib, lambda: A.check(lib.phcu_binary(op, ctypes.byref(xv), ctypes.byref(yv),
-                                                             ctypes.byref(ov))), reps, flush=True)
-            c1["%s_%s" % (name, dt)] = {"ms": round(ms, 4), "gbs": gb(3 * n * 4, ms)}
-        ms = _ms(A, lib, lambda: A.check(lib.phcu_copy(ctypes.byref(gv), ctypes.byref(sv))), reps, flush=True)
-        c1["view_step2_%s" % dt] = {"ms": round(ms, 4), "gbs": gb(2 * (n // 2) * 4, ms)}
+            ms = _flushed_graph_ms(A, lib, lambda: A.check(lib.phcu_binary(op, ctypes.byref(xv), ctypes.byref(yv),
+                                                                           ctypes.byref(ov))))
+            c1["%s_%s" % (name, dt)] = {"ms": round(ms, 5), "gbs": gb(3 * n * 4, ms)}
+        ms = _flushed_graph_ms(A, lib, lambda: A.check(lib.phcu_copy(ctypes.byref(gv), ctypes.byref(sv))))
+        c1["view_step2_%s" % dt] = {"ms": round(ms, 5), "gbs": gb(2 * (n // 2) * 4, ms)}
+    c1["method"] = ("graph of %d (L2 flush, op) pairs minus a graph of %d flushes, median of 5 replays; "
+                    "the op reads its inputs from HBM" % (C1_REPS, C1_REPS))
     res["c1_plain_1024sq"] = c1
 
     # C3: fused ((x+4)**2)*y - z over 64x128x128x64 lognormal, then reductions per axis
@@ -524,20 +640,24 @@ def extra_configs(reps=5):
     ins = (A.View * 3)(*[l._cview() for l in pv._leaves])
     r = cu.CuNArray.empty(shape, cu.Float32)
     rv = r._view()
-    ms = _ms(A, lib, lambda: A.check(lib.phcu_eval(ctypes.byref(prog), ins, 3, ctypes.byref(rv))), reps)
+    # every operand is 256 MiB (twice L2): launches are timed ten back to back per event pair
+    ms = _ms_batched(A, lib, lambda: A.check(lib.phcu_eval(ctypes.byref(prog), ins, 3, ctypes.byref(rv))), reps)
     c3 = {"fused_chain": {"ms": round(ms, 4), "gbs": gb(4 * n3 * 4, ms), "kernels": 1,
-                          "unfused_bytes": 10 * n3 * 4}}
+                          "unfused_bytes": 10 * n3 * 4},
+          "method": "median of 5 event pairs, each around 10 back-to-back launches (operands 256 MiB > L2)"}
     for k in range(4):
         oshape = shape[:k] + shape[k + 1:]
         for name, op, odt in (("sum", A.RED_SUM, cu.Float32), ("max", A.RED_MAX, cu.Float32),
                               ("argmax", A.RED_ARGMAX, cu.Int32)):
             o = cu.CuNArray.empty(oshape, odt)
             oview = o._view()
-            ms = _ms(A, lib, lambda: A.check(lib.phcu_reduce(op, ctypes.byref(rv), k, ctypes.byref(oview))), reps)
+            ms = _ms_batched(A, lib, lambda: A.check(lib.phcu_reduce(op, ctypes.byref(rv), k, ctypes.byref(oview))),
+                             reps)
             c3["%s_axis%d" % (name, k)] = {"ms": round(ms, 4), "gbs": gb(n3 * 4 + o.size * 4, ms)}
     o1 = cu.CuNArray.empty([1], cu.Float32)
     o1v = o1._view()
-    ms = _ms(A, lib, lambda: A.check(lib.phcu_reduce(A.RED_SUM, ctypes.byref(rv), -1, ctypes.byref(o1v))), reps)
+    ms = _ms_batched(A, lib, lambda: A.check(lib.phcu_reduce(A.RED_SUM, ctypes.byref(rv), -1, ctypes.byref(o1v))),
+                     reps)
     c3["sum_all"] = {"ms": round(ms, 4), "gbs": gb(n3 * 4, ms)}
     res["c3_fused_reduce"] = c3
     del x, y, z, r
@@ -599,8 +719,7 @@ def batched_leg(reps=5, n_tasks=10000):
                                             4)}
     allf = tuner.feature_matrix(tasks)
     allpick, _ = net.pick(allf)
-    chunks = [[2048, 8192, 32768, 131072][c % 4] for c in allpick]
-    layouts = [c // 4 for c in allpick]
+    chunks, layouts = tuner.config_args(allpick)
     bt = Batch(wl.tasks(chunks, layouts), wl.programs)
     bt.launch(0)
     ms = _ms(A, lib, lambda: bt.launch(0), reps)
@@ -612,50 +731,79 @@ def batched_leg(reps=5, n_tasks=10000):
 
 
 # ------------------------------------------------------------ CPU baseline
-def cpu_workload(nthreads, shape=CPU_SAMPLE_SHAPE):
-    """The same step on the oracle (the reference's loops restated in C): one
-    materialised pass per operation, per-element view transforms."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as ora
-    from phase_cu import synth
-    from phase_cu.region import R
+CPU_SLABS = 16
 
-    ora.build()
-    n = int(np.prod(shape))
-    total_bytes = 0
-    t0 = time.perf_counter()
-    for dt in ("f32", "i32"):
-        if dt == "f32":
-            a = synth.uniform_f32(shape, seed=0)
-            b = synth.uniform_f32(shape, seed=0, start=n)
-        else:
-            a = synth.uniform_i32(shape, seed=0, lo=-2 ** 20, hi=2 ** 20)
-            b = synth.uniform_i32(shape, seed=0, lo=-2 ** 20, hi=2 ** 20, start=n)
-        es = 4
-        perm = [("permute", [2, 0, 1])]
-        rev = [("region", [slice(None), R(None, None, -1), slice(None)])]
-        ap, bp = ora.ViewOperand(a, perm), ora.ViewOperand(b, perm)
-        ar, br = ora.ViewOperand(a, rev), ora.ViewOperand(b, rev)
-        ora.gather(ap, nthreads)
-        ora.gather(ar, nthreads)
-        total_bytes += 4 * n * es
-        ops = [ora.OP_ADD, ora.OP_SUB, ora.OP_MUL if dt == "f32" else ora.OP_WMUL, ora.OP_DIV]
-        for x, y in ((ap, bp), (ar, br)):
-            for op in ops:
-                ora.map_binary(op, x, y, nthreads)
-                total_bytes += 2 * n * es + n * (8 if (op == ora.OP_DIV and dt == "i32") else es)
-        c = np.zeros([shape[2], shape[0], shape[1]], dtype=a.dtype)
-        ora.scatter(ora.ViewOperand(c, rev), ap)
-        total_bytes += 2 * n * es
-    dt_s = time.perf_counter() - t0
-    return total_bytes / dt_s / 1e9, dt_s, total_bytes
+
+class CpuStep:
+    """The step on the oracle (the reference's loops restated in C: one
+    materialised pass per operation, per-element view transforms) over the
+    full-size arrays.  A bounded sample computes one lexicographic slab (1/16)
+    of every operation's output with every host thread: the same arrays,
+    strides and access pattern as the full step, a sixteenth of its elements."""
+
+    def __init__(self, shape=SHAPE):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as ora
+        from phase_cu import synth
+        from phase_cu.region import R
+
+        ora.build()
+        self.ora = ora
+        self.n = n = int(np.prod(shape))
+        self.ops = []
+        for dt in ("f32", "i32"):
+            if dt == "f32":
+                a = synth.uniform_f32(shape, seed=0)
+                b = synth.uniform_f32(shape, seed=0, start=n)
+            else:
+                a = synth.uniform_i32(shape, seed=0, lo=-2 ** 20, hi=2 ** 20)
+                b = synth.uniform_i32(shape, seed=0, lo=-2 ** 20, hi=2 ** 20, start=n)
+            perm = [("permute", [2, 0, 1])]
+            rev = [("region", [slice(None), R(None, None, -1), slice(None)])]
+            ap, bp = ora.ViewOperand(a, perm), ora.ViewOperand(b, perm)
+            ar, br = ora.ViewOperand(a, rev), ora.ViewOperand(b, rev)
+            out = np.empty(ap.shape, dtype=a.dtype)
+            out64 = np.empty(ap.shape, dtype=np.float64)
+            self.ops.append(("gather", ap, None, out, 8))
+            self.ops.append(("gather", ar, None, out, 8))
+            for x, y in ((ap, bp), (ar, br)):
+                for op in (ora.OP_ADD, ora.OP_SUB, ora.OP_MUL if dt == "f32" else ora.OP_WMUL, ora.OP_DIV):
+                    wide = op == ora.OP_DIV and dt == "i32"
+                    self.ops.append((op, x, y, out64 if wide else out, 16 if wide else 12))
+            c = np.zeros([shape[2], shape[0], shape[1]], dtype=a.dtype)
+            self.ops.append(("scatter", ora.ViewOperand(c, rev), ap, None, 8))
+
+    def run(self, nthreads, slab=0, slabs=1):
+        """Runs slab `slab` of `slabs` of every operation; returns (seconds, algorithmic bytes)."""
+        ora, n = self.ora, self.n
+        lo, hi = n * slab // slabs, n * (slab + 1) // slabs
+        t0 = time.perf_counter()
+        for kind, x, y, out, per in self.ops:
+            if kind == "gather":
+                ora.gather_range(x, out, lo, hi, nthreads)
+            elif kind == "scatter":
+                ora.scatter_range(x, y, lo, hi, nthreads)
+            else:
+                ora.map_binary_range(kind, x, y, out, lo, hi, nthreads)
+        return time.perf_counter() - t0, sum(o[4] for o in self.ops) * (hi - lo)
 
 
 def cpu_baseline(nthreads):
-    gbs, secs, nbytes = cpu_workload(nthreads)
-    return {"value": round(gbs, 3), "unit": "GB/s", "cores": nthreads, "kind": "port",
-            "sample": "the same step on Float32+Int32 %s arrays (1/64 of the elements), %.1f s, %d algorithmic bytes"
-                      % ("x".join(map(str, CPU_SAMPLE_SHAPE)), secs, nbytes)}
+    """Two slab samples (1/16 each) of the full-size step on the oracle with
+    every host thread, and (for scale) the reference's own single thread on
+    one slab."""
+    step = CpuStep()
+    secs, nbytes = 0.0, 0
+    for k in range(2):
+        t, b = step.run(nthreads, k, CPU_SLABS)
+        secs += t
+        nbytes += b
+    t1, b1 = step.run(1, 2, CPU_SLABS)
+    return {"value": round(nbytes / secs / 1e9, 3), "unit": "GB/s", "cores": nthreads, "kind": "port",
+            "sample": "slabs 0-1 of %d of every operation's output on the full-size step (Float32+Int32 %s), "
+                      "%.1f s, %d algorithmic bytes" % (CPU_SLABS, "x".join(map(str, SHAPE)), secs, nbytes),
+            "single_thread": {"value": round(b1 / t1 / 1e9, 3), "cores": 1,
+                              "sample": "slab 2 of %d, %.1f s" % (CPU_SLABS, t1)}}
 
 
 def reference_arm(args):
@@ -663,23 +811,25 @@ def reference_arm(args):
     if rank != 0:
         return None, rank
     threads = os.cpu_count() or 1
+    step = CpuStep()
+    for k in range(args.warmup):
+        step.run(threads, k % CPU_SLABS, CPU_SLABS)
     vals = []
-    for _ in range(args.warmup):
-        cpu_workload(threads)
-    for _ in range(args.steps):
-        gbs, secs, nbytes = cpu_workload(threads)
-        vals.append((gbs, secs, nbytes))
-    gbs = sum(v[2] for v in vals) / sum(v[1] for v in vals) / 1e9
-    ms = 1e3 * sum(v[1] for v in vals) / len(vals)
+    for k in range(args.steps):
+        vals.append(step.run(threads, k % CPU_SLABS, CPU_SLABS))
+    gbs = sum(v[1] for v in vals) / sum(v[0] for v in vals) / 1e9
+    ms = 1e3 * sum(v[0] for v in vals) / len(vals)
     res = {"impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": "GB/s", "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32", "data": "synthetic (SplitMix64, seed 0)",
-           "config": {"workload": WORKLOAD, "shape": SHAPE, "sample_shape": CPU_SAMPLE_SHAPE,
-                      "l2": "n/a (CPU)", "parallelism": "host threads"},
+           "config": bench_config(),
+           "execution": "oracle port of the reference loops on %d host threads" % threads,
            "cpu_baseline": {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
-                            "sample": "each step = the step on %s arrays (1/64 of the elements); the reference is "
-                                      "Crystal and cannot be built here, so its loops run as the C oracle"
-                                      % "x".join(map(str, CPU_SAMPLE_SHAPE))},
+                            "sample": "step k = slab k mod %d (1/%d of the elements, a contiguous lexicographic "
+                                      "range) of every operation's output on the full-size arrays (Float32+Int32 "
+                                      "%s), every host thread; the reference is Crystal and cannot be built here, "
+                                      "so its loops run as the C oracle (one materialised pass per operation, "
+                                      "per-element view transforms)" % (CPU_SLABS, CPU_SLABS, "x".join(map(str, SHAPE)))},
            "e2e": {"value": round(gbs, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     return res, rank
 
@@ -696,8 +846,11 @@ def main():
                    help="run only one operation class (gather_permute, gather_reverse, binary_permute, "
                         "binary_reverse, binary_permute_div_i32, binary_reverse_div_i32, scatter) for profiling")
     p.add_argument("--profile-dtype", default="f32")
-    p.add_argument("--profile-config", default=None, choices=["c3", "c4"],
-                   help="one untimed pass of the fused-chain/reduction (c3) or heat (c4) workload, for profiling")
+    p.add_argument("--profile-shape", default=None,
+                   help="a smaller AxBxC shape for --profile-class (ncu captures of several metrics)")
+    p.add_argument("--profile-config", default=None, choices=["c3", "c4", "c5"],
+                   help="one untimed pass of the fused-chain/reduction (c3), heat (c4) or batch (c5) workload, "
+                        "for profiling")
     args = p.parse_args()
     if args.profile_class:
         profile_class(args)
