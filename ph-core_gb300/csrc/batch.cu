@@ -30,7 +30,7 @@
 namespace phcu {
 
 int32_t launch_eval_plan(const EvalPlan& plan, const phcu_program_t& prog);  // eval.cu
-int32_t launch_reduce_plan(const RedArgs& a, int mode, int G, int vec);       // reduce.cu
+int32_t launch_reduce_pooled(RedArgs a, const RedShape& sh);                  // reduce.cu
 
 constexpr int64_t DEFAULT_CHUNK = 16384;  // elements per work item
 constexpr int64_t WALK_ELEMS = 512;       // reduced elements one thread walks per unit, about at most
@@ -40,8 +40,15 @@ static BatchKernel pick_kernel(bool narrow, int nin, bool wide) {
   return batch_kernel_u64();
 }
 
+// The per-op replay of a reduction task: the standalone plan and launch shape.
+struct Replay {
+  RedArgs ra;
+  RedShape sh;
+};
+
 struct Batch {
   std::vector<BTask> host_tasks;
+  std::vector<Replay> replays;  // indexed by BTask::pad of reduction tasks
   std::vector<phcu_program_t> host_progs;
   BTask* d_tasks = nullptr;
   int32_t* d_item_task = nullptr;
@@ -193,6 +200,12 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
         if (rmode == 1 && bt.ra.orank == 0) rmode = 0;
         bt.h.rmode = rmode;
         bt.h.rG = rmode == 0 ? (rmode == sh.mode ? sh.G : 32) : 1;
+        // the per-op replay runs the standalone plan (its splits and, in the
+        // planner's layout, its vector loads) in the chosen layout
+        Replay rp{bt.ra, sh};
+        if (rmode != sh.mode) rp.sh = RedShape{rmode, rmode == 0 ? 32 : 1, 0};
+        bt.pad = (int32_t)b->replays.size();
+        b->replays.push_back(rp);
         if (dtype_size(bt.ra.dtype) == 8) wide = true;
         batch_splits(bt.ra, rmode, bt.h.rG);
         bt.h.nunits = bt.ra.O * bt.ra.S;
@@ -313,7 +326,7 @@ int32_t batch_launch(Batch* b, int mode) {
   unsigned long long before = ctx().launches;
   int32_t rc = PHCU_OK;
   for (const BTask& bt : b->host_tasks) {
-    if (bt.h.kind == BK_REDUCE) rc = launch_reduce_plan(bt.ra, bt.h.rmode, bt.h.rmode == 1 ? 1 : bt.h.rG, 0);
+    if (bt.h.kind == BK_REDUCE) rc = launch_reduce_pooled(b->replays[(size_t)bt.pad].ra, b->replays[(size_t)bt.pad].sh);
     else rc = launch_eval_plan(bt.ep, b->host_progs[bt.prog]);
     if (rc != PHCU_OK) break;
   }

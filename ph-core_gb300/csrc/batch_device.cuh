@@ -32,7 +32,7 @@ struct BHead {
 struct BTask {
   BHead h;
   int32_t prog;
-  int32_t pad;
+  int32_t pad;  // reduction: index of its per-op replay plan (host side)
   int64_t bytes;
   int64_t order_key;
   EvalPlan ep;

@@ -188,13 +188,17 @@ static int32_t launch_reduce(const RedArgs& a, const RedShape& sh) {
   }
 }
 
-// Launches an already planned reduction (used by the batched executor's per-op replay).
-int32_t launch_reduce_plan(const RedArgs& a, int mode, int G, int vec) {
-  RedShape sh;
-  sh.mode = mode;
-  sh.G = G;
-  sh.vec = vec;
-  return launch_reduce(a, sh);
+// Launches an already planned reduction the way phcu_reduce does, split
+// partials in stream-ordered pool scratch (the batched executor's per-op replay).
+int32_t launch_reduce_pooled(RedArgs a, const RedShape& sh) {
+  void* scratch = nullptr;
+  if (a.S > 1) {
+    PHCU_TRY(scratch_alloc((size_t)a.S * (size_t)a.O * sizeof(Partial), &scratch));
+    a.partial = (Partial*)scratch;
+  }
+  const int32_t rc = launch_reduce(a, sh);
+  if (scratch) scratch_free(scratch);
+  return rc;
 }
 
 static void merge_axes(int64_t* sh, int64_t* st, int& rank, bool keep_one) {

@@ -397,6 +397,80 @@ inline std::vector<int64_t> row_major(const std::vector<int64_t>& shape) {
   return st;
 }
 
+namespace detail {
+// Whether writing `src` into `dst` (two layouts over one buffer, equal element
+// counts) element by element in lexicographic order, as the reference's
+// MultiWritable#unsafe_set_chunk does (multi_writable.cr:29-44), can differ
+// from reading the whole source first, as the device does: some element is
+// read at step i after a step j < i changed it (S(i) = D(j), S(j) != D(j)).
+// Exact up to 2^22 elements; above, false only for a destination walked in
+// increasing address order whose every read is at or past the write of its
+// step.  A destination that writes an element twice counts as differing.
+inline bool sequential_order_differs(const Affine& dst, const Affine& src) {
+  std::vector<std::pair<int64_t, int64_t>> d, s;  // (extent, stride) of the non-unit axes
+  for (size_t i = 0; i < dst.shape.size(); i++)
+    if (dst.shape[i] != 1) d.push_back({dst.shape[i], dst.stride[i]});
+  for (size_t i = 0; i < src.shape.size(); i++)
+    if (src.shape[i] != 1) s.push_back({src.shape[i], src.stride[i]});
+  int64_t n = 1;
+  for (auto& a : d) n *= a.first;
+  if (n == 0) return false;
+  if (dst.offset == src.offset && d == s) return false;  // each step reads the element it writes
+  auto span = [](const std::vector<std::pair<int64_t, int64_t>>& v, int64_t off, int64_t* lo, int64_t* hi) {
+    *lo = *hi = off;
+    for (auto& a : v) {
+      const int64_t e = (a.first - 1) * a.second;
+      if (e < 0) *lo += e;
+      else *hi += e;
+    }
+  };
+  int64_t dlo, dhi, slo, shi;
+  span(d, dst.offset, &dlo, &dhi);
+  span(s, src.offset, &slo, &shi);
+  if (shi < dlo || dhi < slo) return false;  // disjoint
+  auto addresses = [n](const std::vector<std::pair<int64_t, int64_t>>& v, int64_t off) {
+    std::vector<int64_t> a(1, off);
+    a.reserve((size_t)n);
+    for (auto& ax : v) {
+      std::vector<int64_t> b;
+      b.reserve(a.size() * (size_t)ax.first);
+      for (int64_t x : a)
+        for (int64_t k = 0; k < ax.first; k++) b.push_back(x + k * ax.second);
+      a.swap(b);
+    }
+    return a;
+  };
+  if (n <= ((int64_t)1 << 22)) {
+    const std::vector<int64_t> da = addresses(d, dst.offset), sa = addresses(s, src.offset);
+    std::vector<std::pair<int64_t, int64_t>> order((size_t)n);  // (address, step)
+    for (int64_t j = 0; j < n; j++) order[(size_t)j] = {da[(size_t)j], j};
+    std::sort(order.begin(), order.end());
+    for (size_t k = 1; k < order.size(); k++)
+      if (order[k].first == order[k - 1].first) return true;  // an element written twice
+    for (int64_t i = 0; i < n; i++) {
+      auto it = std::lower_bound(order.begin(), order.end(), std::make_pair(sa[(size_t)i], (int64_t)INT64_MIN));
+      if (it == order.end() || it->first != sa[(size_t)i]) continue;
+      const int64_t j = it->second;
+      if (j < i && sa[(size_t)j] != da[(size_t)j]) return true;
+    }
+    return false;
+  }
+  bool monotone = true;
+  int64_t inner = 0;
+  for (size_t k = d.size(); k-- > 0;) {
+    monotone = monotone && d[k].second > inner;
+    inner += (d[k].first - 1) * d[k].second;
+  }
+  if (!monotone || d.size() != s.size()) return true;
+  int64_t gap = src.offset - dst.offset;
+  for (size_t k = 0; k < d.size(); k++) {
+    if (d[k].first != s[k].first) return true;
+    gap += std::min<int64_t>(0, (d[k].first - 1) * (s[k].second - d[k].second));
+  }
+  return gap < 0;
+}
+}  // namespace detail
+
 inline phcu_view_t make_view(void* base, int32_t dtype, const Affine& a) {
   if (a.shape.size() > (size_t)PHCU_MAX_RANK)
     throw DimensionError("rank " + std::to_string(a.shape.size()) + " exceeds the device limit of " +
@@ -551,19 +625,28 @@ class CuNArray : public CuView<T> {
     const CuView<T> dst = this->view(region);
     if (dst.shape() != src.shape())
       throw ShapeError("Cannot set chunk: the source's shape differs from the region's shape.");
+    refuse_reordered_alias(dst, src.buffer().get(), src.layout());
     const phcu_view_t d = dst.desc(), s = src.desc();
     check(phcu_copy(&d, &s), "phcu_copy");
   }
   void set_chunk(const std::vector<Lit>& region, T value) { fill_view(this->view(region).desc(), value); }
-  // A fused source is materialised first (it may read the region it writes,
-  // as the heat step does), then copied in.
-  void set_chunk(const std::vector<Lit>& region, const CuProcView<T>& src) { set_chunk(region, src.to_cu()); }
+  // A fused source is evaluated first, then copied in.  The reference reads
+  // its operands element by element while it writes, so an operand that
+  // aliases the region in another element order is refused.
+  void set_chunk(const std::vector<Lit>& region, const CuProcView<T>& src);
 
  private:
   static int64_t count(const std::vector<int64_t>& shape) {
     for (int64_t s : shape)
       if (s < 0) throw DimensionError("Cannot create NArray: One or more of the provided dimensions was negative.");
     return shape.empty() ? 1 : shape_to_size(shape);
+  }
+  static void refuse_reordered_alias(const CuView<T>& dst, const Buffer* src_buf, const Affine& src) {
+    if (src_buf == dst.buffer().get() && detail::sequential_order_differs(dst.layout(), src))
+      throw NotImplementedError(
+          "set_chunk: the source overlaps the destination in another element order, so the reference's "
+          "element-by-element write would read elements it has already written, while the device reads the "
+          "whole source first; write a copy of the source (clone) instead");
   }
   static void fill_view(const phcu_view_t& v, T value) {
     phcu_scalar_t s;
@@ -1146,6 +1229,13 @@ class CuProcView {
   detail::ExprP expr_;
   std::vector<int64_t> shape_;
 };
+
+template <typename T>
+void CuNArray<T>::set_chunk(const std::vector<Lit>& region, const CuProcView<T>& src) {
+  const CuView<T> dst = this->view(region);
+  for (const detail::Leaf& l : src.leaves()) refuse_reordered_alias(dst, l.buf.get(), l.aff);
+  set_chunk(region, src.to_cu());
+}
 
 template <typename T>
 CuProcView<T> CuView<T>::process() const {

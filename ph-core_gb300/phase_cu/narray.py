@@ -503,6 +503,10 @@ class _Indexable:
         if not isinstance(self, (CuNArray, CuMutableView)):
             raise NotImplementedError("%s is read-only: in-place maps need a CuNArray or a CuMutableView"
                                       % type(self).__name__)
+        mine = self._desc()
+        for leaf in pv._leaves:
+            if not isinstance(leaf, CuIndexView):
+                _refuse_reordered_alias(mine, leaf._desc(), "in-place map")
         out = self._cview()
         pv._eval_into(out, self.dtype)
         return self
@@ -1045,13 +1049,95 @@ class CuNArray(_Indexable):
 
 
 
+# Above this many elements, an overlapping write is classified by the
+# address-order rule only (the exact check walks every element on the host).
+_ALIAS_EXACT_LIMIT = 1 << 22
+
+
+def _lex_addresses(off, shape, stride):
+    """Element offsets of an affine view in lexicographic order (int64)."""
+    a = np.full([1], off, dtype=np.int64)
+    for n, st in zip(shape, stride):
+        a = (a[:, None] + np.arange(n, dtype=np.int64)[None, :] * st).reshape(-1)
+    return a
+
+
+def _sequential_order_differs(dst, src):
+    """Whether writing `src` into `dst` element by element in lexicographic
+    order (MultiWritable#unsafe_set_chunk, multi_writable.cr:29-44; Mutable#map_with!,
+    mutable.cr:54-67) can give other results than reading every source
+    element first, which is what the device does (it stages an overlapping
+    source).  dst and src are (buffer, offset, shape, stride) of one element
+    size with equal element counts.  They differ when some element is read at
+    step i after a step j < i changed it: S(i) = D(j) with S(j) != D(j) (a
+    step that reads and writes the same element changes nothing; a
+    destination that writes an element twice is always refused).  Above
+    _ALIAS_EXACT_LIMIT elements the answer is conservative: False only when
+    the destination is walked in increasing address order and every read
+    stays at or ahead of the write of its step."""
+    dbuf, doff, dshape, dstride = dst
+    sbuf, soff, sshape, sstride = src
+    if dbuf is None or sbuf is None or dbuf.ptr != sbuf.ptr:
+        return False
+    dsh = [(n, st) for n, st in zip(dshape, dstride) if n != 1]
+    ssh = [(n, st) for n, st in zip(sshape, sstride) if n != 1]
+    n = shape_to_size(list(dshape))
+    if n == 0:
+        return False
+    if doff == soff and dsh == ssh:
+        return False  # the same mapping: each step reads the element it writes
+    lo_d = doff + sum(min(0, (k - 1) * st) for k, st in dsh)
+    hi_d = doff + sum(max(0, (k - 1) * st) for k, st in dsh)
+    lo_s = soff + sum(min(0, (k - 1) * st) for k, st in ssh)
+    hi_s = soff + sum(max(0, (k - 1) * st) for k, st in ssh)
+    if hi_s < lo_d or hi_d < lo_s:
+        return False  # disjoint
+    if n <= _ALIAS_EXACT_LIMIT:
+        d = _lex_addresses(doff, [x[0] for x in dsh], [x[1] for x in dsh])
+        s_ = _lex_addresses(soff, [x[0] for x in ssh], [x[1] for x in ssh])
+        order = np.argsort(d, kind="stable")
+        ds = d[order]
+        if ds.size > 1 and np.any(ds[1:] == ds[:-1]):
+            return True  # the destination writes some element twice
+        pos = np.minimum(np.searchsorted(ds, s_), ds.size - 1)
+        hit = ds[pos] == s_
+        j = order[pos]
+        changed = s_[j] != d[j]
+        return bool(np.any(hit & (j < np.arange(n)) & changed))
+    # large views: a destination walked in increasing address order (positive
+    # strides, each larger than the span of the axes inside it) whose every
+    # read S(i) is at or past D(i) never reads an element already written
+    monotone = all(st > 0 for _, st in dsh)
+    inner = 0
+    for k, st in reversed(dsh):
+        monotone = monotone and st > inner
+        inner += (k - 1) * st
+    if not monotone or [x[0] for x in dsh] != [x[0] for x in ssh]:
+        return True
+    gap = soff - doff + sum(min(0, (k - 1) * (ss - ds)) for (k, ds), (_, ss) in zip(dsh, ssh))
+    return gap < 0
+
+
+def _refuse_reordered_alias(dst, src, what):
+    if _sequential_order_differs(dst, src):
+        raise NotImplementedError(
+            "%s: the source overlaps the destination in another element order, so the reference's "
+            "element-by-element write would read elements it has already written, while the device reads "
+            "the whole source first; write a copy of the source (clone) instead" % what)
+
+
 def _write_region(target, region, src):
     """unsafe_set_chunk (n_array.cr:484-500; multi_writable.cr:29-44) with a
     device source (gather/scatter kernel) or a scalar (fill kernel)."""
-    if isinstance(src, CuProcView):
-        src = src.to_cu()
     buf, off, shape, stride = target._desc()
     o, s, st = _affine_region(off, shape, stride, region)
+    if isinstance(src, CuProcView):
+        # the reference reads the ProcView's operands element by element while
+        # it writes: an operand aliasing the region in another order is refused
+        for leaf in src._leaves:
+            if not isinstance(leaf, CuIndexView):
+                _refuse_reordered_alias((buf, o, s, st), leaf._desc(), "set_chunk")
+        src = src.to_cu()
     dview = _make_view(buf, target.dtype, o, s, st)
     if isinstance(src, _Indexable):
         if not compatible_shapes(src.shape, region.shape):
@@ -1059,6 +1145,7 @@ def _write_region(target, region, src):
                              % (type(src).__name__, type(src).__name__, src.shape, region, region.shape))
         if src.dtype != target.dtype:
             src = src.to_cu()._astype(target.dtype)
+        _refuse_reordered_alias((buf, o, s, st), src._desc(), "set_chunk")
         _copy_into(dview, src._cview())
     else:
         sv = A.Scalar()

@@ -132,8 +132,14 @@ class MLP:
                                      ctypes.byref(loss)), "phcu_mlp_train")
         return loss.value
 
-    def pick(self, feats):
-        """feats [tasks, configs, 24] -> configuration with the smallest predicted time."""
+    def pick(self, feats, default=DEFAULT_CONFIG, margin=0.1):
+        """feats [tasks, configs, 24] -> the configuration with the smallest
+        predicted time, or `default` when the network predicts no gain of at
+        least `margin` (relative) over it: many tasks run in a few
+        microseconds under every configuration, where a predicted difference
+        is mostly timing noise and the default is as good a choice."""
         t, c, f = feats.shape
         pred = self.forward(feats.reshape(-1, f)).reshape(t, c)
-        return np.argmin(pred, axis=1), pred
+        best = np.argmin(pred, axis=1)
+        gain = pred[:, default] - pred[np.arange(t), best]  # log2 of the predicted speed-up
+        return np.where(gain >= np.log2(1.0 + margin), best, default), pred

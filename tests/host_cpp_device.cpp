@@ -103,8 +103,16 @@ static void run_proc(const std::string& tag) {
   C.set_chunk(rev, A.process() + B);
   save(tag + "_proc_set", C.to_vector());
   CuNArray<T> D = A.clone();
-  D.set_chunk({rng(1, -1)}, D.view({rng(0, -2)}).process() * 2);  // reads the rows it writes
+  // a source one row ahead of the rows it writes: element by element, every
+  // read comes before the write that reaches it, so the result is the reference's
+  D.set_chunk({rng(0, -2)}, D.view({rng(1, -1)}).process() * 2);
   save(tag + "_proc_overlap", D.to_vector());
+  // one row behind: the reference would read rows it has already written
+  expect_raise(tag + "_proc_overlap_behind", [&] {
+    CuNArray<T> E = A.clone();
+    E.set_chunk({rng(1, -1)}, E.view({rng(0, -2)}).process() * 2);
+    return E;
+  });
   save(tag + "_proc_const", A.process([](auto) { return 2.5f; }).to_vector());
   // five distinct operand views (A, B, A and B reversed on axis 1, A reversed
   // on every axis; CuView - CuView alone would be eager): more than one device

@@ -180,8 +180,10 @@ def test_fused_chains(run_proc, ora, tag):
     c[:, ::-1, :] = ora.map_binary(ora.OP_ADD, a, b)[0]
     assert np.array_equal(load(tag + "_proc_set", dt), c.reshape(-1))
     d = a.copy()
-    d[1:] = ora.map_binary_scalar(ora.OP_MUL, np.ascontiguousarray(a[:-1]), 2, t)[0]
+    d[:-1] = ora.map_binary_scalar(ora.OP_MUL, np.ascontiguousarray(a[1:]), 2, t)[0]
     assert np.array_equal(load(tag + "_proc_overlap", dt), d.reshape(-1))
+    # the reference's element order would read rows already written: refused
+    assert "raised %s_proc_overlap_behind NotImplementedError" % tag in lines
     assert np.all(load(tag + "_proc_const", np.float32) == np.float32(2.5))
     # five operand views: split into two device programs, same results
     five, _ = ora.map_binary(ora.OP_ADD, a, b)
