@@ -355,7 +355,11 @@ PHCU_API int32_t phcu_batch_run(const phcu_task_t* tasks, int32_t n_tasks, const
 PHCU_API int32_t phcu_tune_n_configs(int32_t* n);
 /* Feature vector of (task, config) as the tuner sees it. */
 PHCU_API int32_t phcu_tune_features(const phcu_task_t* task, int32_t config, float* features);
-/* Times `task` under every config (reps each, median); ms[n_configs]. */
+/* Times `task` under every config (reps each, median); ms[n_configs].  The
+ * task runs as a batch of copies that fills the GPU (up to 512, about 2^22
+ * elements in all), and ms is the time per copy: its cost inside a large
+ * batch.  The task runs (reps + 1) x copies times per config, so an in-place
+ * task changes its data. */
 PHCU_API int32_t phcu_tune_measure(const phcu_task_t* task, const phcu_program_t* programs, int32_t reps,
                           float* ms);
 /* Runs `task` once under `config` (standalone kernels). */

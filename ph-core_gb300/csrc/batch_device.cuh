@@ -40,7 +40,17 @@ struct BTask {
 };
 
 constexpr int BATCH_THREADS = 256;
-constexpr int BATCH_MIN_BLOCKS = 3;
+#ifndef PHCU_BATCH_MIN_BLOCKS
+#define PHCU_BATCH_MIN_BLOCKS 3
+#endif
+constexpr int BATCH_MIN_BLOCKS = PHCU_BATCH_MIN_BLOCKS;
+// Bodies are separate functions (each its own register allocation) unless
+// PHCU_BATCH_INLINE is defined.
+#ifdef PHCU_BATCH_INLINE
+#define PHCU_BODY __forceinline__
+#else
+#define PHCU_BODY __noinline__
+#endif
 
 __device__ __forceinline__ uint64_t global_ns() {
   uint64_t t;
@@ -75,22 +85,38 @@ __device__ __forceinline__ void row_fast(const BHead& h, const EvalPlan& p, cons
   else row_item<S, NIN, 1, V / 2, STASH, FAST>(p, prog, u0, u1, st);
 }
 
+// One function per body and chunk width: each gets its own register allocation.
+template <typename S, int NIN, int VEC, int FAST>
+__device__ PHCU_BODY void run_row_body(const EvalPlan& p, const phcu_program_t& prog, int64_t u0, int64_t u1,
+                                          uint32_t& st) {
+  constexpr int V = batch_v<S, FAST>();
+  row_item<S, NIN, VEC, VEC == 4 ? V / 4 : V / 2, FAST == FAST_NONE, FAST>(p, prog, u0, u1, st);
+}
+
 template <typename S, int NIN>
-__device__ __noinline__ void run_row(const BHead& h, const EvalPlan& p, const phcu_program_t& prog, int64_t u0,
-                                     int64_t u1, uint32_t& st) {
-  if (h.fast == FAST_FX) row_fast<S, NIN, FAST_FX>(h, p, prog, u0, u1, st);
-  else row_fast<S, NIN, FAST_NONE>(h, p, prog, u0, u1, st);
+__device__ __forceinline__ void run_row(const BHead& h, const EvalPlan& p, const phcu_program_t& prog, int64_t u0,
+                                        int64_t u1, uint32_t& st) {
+  if (h.fast == FAST_FX) {
+    if (h.vec == 4) run_row_body<S, NIN, 4, FAST_FX>(p, prog, u0, u1, st);
+    else run_row_body<S, NIN, 1, FAST_FX>(p, prog, u0, u1, st);
+  } else {
+    if (h.vec == 4) run_row_body<S, NIN, 4, FAST_NONE>(p, prog, u0, u1, st);
+    else run_row_body<S, NIN, 1, FAST_NONE>(p, prog, u0, u1, st);
+  }
 }
 
 // ----------------------------------------------------------- TILE bodies
+template <typename S, int NIN, int FAST>
+__device__ PHCU_BODY void run_tile_body(const EvalPlan& p, const phcu_program_t& prog, int64_t u0, int64_t u1,
+                                           S* tiles, uint32_t& st) {
+  for (int64_t t = u0; t < u1; t++) tile_body<S, NIN, FAST == FAST_NONE, FAST>(p, prog, (uint64_t)t, tiles, st);
+}
+
 template <typename S, int NIN>
-__device__ __noinline__ void run_tile(const BHead& h, const EvalPlan& p, const phcu_program_t& prog, int64_t u0,
-                                      int64_t u1, S* tiles, uint32_t& st) {
-  if (h.fast == FAST_FX) {
-    for (int64_t t = u0; t < u1; t++) tile_body<S, NIN, false, FAST_FX>(p, prog, (uint64_t)t, tiles, st);
-  } else {
-    for (int64_t t = u0; t < u1; t++) tile_body<S, NIN, true, FAST_NONE>(p, prog, (uint64_t)t, tiles, st);
-  }
+__device__ __forceinline__ void run_tile(const BHead& h, const EvalPlan& p, const phcu_program_t& prog, int64_t u0,
+                                         int64_t u1, S* tiles, uint32_t& st) {
+  if (h.fast == FAST_FX) run_tile_body<S, NIN, FAST_FX>(p, prog, u0, u1, tiles, st);
+  else run_tile_body<S, NIN, FAST_NONE>(p, prog, u0, u1, tiles, st);
 }
 
 // ------------------------------------------------------ REDUCE bodies
@@ -121,7 +147,7 @@ __device__ __forceinline__ void red_combine(const RedArgs& a, CombineScratch& cs
 }
 
 template <bool WIDE>
-__device__ __noinline__ void run_reduce(const BHead& h, const RedArgs& a, int64_t u0, int64_t u1, uint32_t& st) {
+__device__ PHCU_BODY void run_reduce(const BHead& h, const RedArgs& a, int64_t u0, int64_t u1, uint32_t& st) {
   const bool sum = a.op == PHCU_RED_SUM;
   switch (a.dtype) {
     case PHCU_F32:
@@ -147,7 +173,7 @@ __device__ __noinline__ void run_reduce(const BHead& h, const RedArgs& a, int64_
 }
 
 template <bool WIDE>
-__device__ __noinline__ void run_combine(const RedArgs& a, CombineScratch& cs, uint32_t& st) {
+__device__ PHCU_BODY void run_combine(const RedArgs& a, CombineScratch& cs, uint32_t& st) {
   const bool sum = a.op == PHCU_RED_SUM;
   switch (a.dtype) {
     case PHCU_F32:

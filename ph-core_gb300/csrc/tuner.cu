@@ -246,12 +246,20 @@ int32_t phcu_tune_measure(const phcu_task_t* task, const phcu_program_t* program
     cudaEventDestroy(e0);
     return cuda_fail(ce, "cudaEventCreate(tune_measure)");
   }
+  // The task is timed as a batch of R copies that together fill the GPU, and
+  // the time is divided by R: a task's cost inside a large batch (its work
+  // items interleave with everyone else's) is its share of the throughput,
+  // not the latency of a launch that it has to itself.
+  const phcu_view_t& src = (task->kind == PHCU_TASK_EVAL && task->n_inputs == 0) ? task->out : task->in[0];
+  const int64_t n = std::max<int64_t>(1, view_size(&src));
+  const int R = (int)std::min<int64_t>(512, std::max<int64_t>(1, ((int64_t)1 << 22) / n));
   int32_t rc = PHCU_OK;
   for (int c = 0; c < NCONF && rc == PHCU_OK; c++) {
     phcu_task_t t = *task;
     apply_config(&t, c);
+    std::vector<phcu_task_t> copies((size_t)R, t);
     void* b = nullptr;
-    rc = phcu_batch_prepare(&t, 1, programs, nprog, &b);
+    rc = phcu_batch_prepare(copies.data(), R, programs, nprog, &b);
     if (rc != PHCU_OK) break;
     rc = phcu_batch_launch(b, 0);  // warm-up
     std::vector<float> v;
@@ -267,7 +275,7 @@ int32_t phcu_tune_measure(const phcu_task_t* task, const phcu_program_t* program
     phcu_batch_destroy(b);
     if (rc == PHCU_OK) {
       std::sort(v.begin(), v.end());
-      ms[c] = v[v.size() / 2];
+      ms[c] = v[v.size() / 2] / (float)R;
     }
   }
   cudaEventDestroy(e0);
