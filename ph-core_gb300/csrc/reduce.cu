@@ -16,6 +16,9 @@
 //            are consecutive in memory, and each thread walks the reduced axis.
 // When there are too few outputs to fill the GPU the reduced axis is split into S
 // pieces; the pieces' partials go to scratch and a combine kernel folds them in order.
+#include <algorithm>
+
+#include "async_copy.cuh"
 #include "reduce_device.cuh"
 
 namespace phcu {
@@ -105,6 +108,270 @@ __global__ void __launch_bounds__(256) reduce_combine_block_kernel(const __grid_
   if (st) atomicOr(a.status, st);
 }
 
+// Full reduction of one contiguous, 16-byte aligned run of K elements in one
+// launch: block b folds a contiguous range of whole vectors (each thread takes
+// vectors t, t + 256, ... in order, four in flight), the block's lanes combine
+// in a fixed tree, thread 0 stores the block's partial (slot b of S = gridDim
+// partials), and the block that arrives last (counter after __threadfence)
+// folds the S partials in block order, stores the result and resets the
+// counter.  The last block also takes the K % VN elements past the last vector.
+template <typename T, int KIND>
+__global__ void __launch_bounds__(256) reduce_all_kernel(const __grid_constant__ RedArgs a, unsigned* arrive) {
+  constexpr int VN = 16 / sizeof(T);
+  __shared__ CombineScratch cs;
+  __shared__ int last;
+  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
+  const int64_t nv = a.K / VN;
+  const int64_t per = (nv + gridDim.x - 1) / gridDim.x;
+  const int64_t v0 = (int64_t)blockIdx.x * per, v1 = min(nv, v0 + per);
+  uint32_t st = 0;
+  SumAcc<T> sacc;
+  ExtAcc<T> eacc;
+  sacc.init();
+  eacc.init();
+  int64_t v = v0 + threadIdx.x;
+  for (; v + 3 * (int64_t)blockDim.x < v1; v += 4 * (int64_t)blockDim.x) {
+    T x[4][VN];
+#pragma unroll
+    for (int u = 0; u < 4; u++) ld16<T>(a.in + (v + u * (int64_t)blockDim.x) * 16, x[u]);
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (KIND == RK_SUM) {
+#pragma unroll
+        for (int e = 0; e < VN; e++) sacc.add(x[u][e]);
+      } else {
+        vec_extreme_into<T, VN>(eacc, x[u], (v + u * (int64_t)blockDim.x) * VN, is_max);
+      }
+    }
+  }
+  for (; v < v1; v += blockDim.x) {
+    T x[VN];
+    ld16<T>(a.in + v * 16, x);
+    if (KIND == RK_SUM) {
+#pragma unroll
+      for (int e = 0; e < VN; e++) sacc.add(x[e]);
+    } else {
+      vec_extreme_into<T, VN>(eacc, x, v * VN, is_max);
+    }
+  }
+  if (blockIdx.x == gridDim.x - 1) {  // the elements past the last whole vector
+    const int64_t k = nv * VN + threadIdx.x;
+    if (k < a.K) {
+      const T x = ld<T>(a.in + k * (int64_t)sizeof(T));
+      if (KIND == RK_SUM) sacc.add(x);
+      else eacc.add(x, k, is_max);
+    }
+  }
+  // lanes of a warp, then the warps in order
+#pragma unroll
+  for (int d = 16; d >= 1; d >>= 1) {
+    if (KIND == RK_SUM) sacc.shfl(d, 0xffffffffu, 32);
+    else eacc.shfl(d, 0xffffffffu, 32, is_max);
+  }
+  __shared__ SumAcc<T> ws[32];
+  __shared__ ExtAcc<T> we[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0) {
+    ws[warp] = sacc;
+    we[warp] = eacc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < nw; w++) {
+      if (KIND == RK_SUM) ws[0].merge(ws[w]);
+      else we[0].merge(we[w], is_max);
+    }
+    RedArgs b = a;
+    b.S = gridDim.x;
+    finish<T, KIND>(b, 0, blockIdx.x, ws[0], we[0], st);  // the block's partial, slot blockIdx.x
+    __threadfence();
+    last = atomicAdd(arrive, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    RedArgs b = a;
+    b.S = gridDim.x;
+    b.O = 1;
+    combine_block<T, KIND>(b, 0, cs, st);
+    if (threadIdx.x == 0) *arrive = 0;
+  }
+  if (st) atomicOr(a.status, st);
+}
+
+// ------------------------------------------------ rows staged by bulk copies
+// Reductions of short contiguous rows laid back to back (the innermost axis of
+// a contiguous array; 4-byte elements, rows of 32-96 elements): a persistent
+// block takes tiles of ROWS_PER_TILE rows; one thread issues one bulk copy of
+// the whole tile (contiguous, 16-byte aligned) into a two-stage ring and the
+// copy of tile i + 2 as soon as every thread has finished tile i.  Thread r
+// reduces row r from shared memory: its vectors are read starting at vector
+// r (mod the row's vector count), so the eight threads of a quarter-warp hit
+// eight different bank groups.  Per element a sum costs its compensated add
+// and an extremum one min/max plus a compare and a select (the first index
+// holding the extreme value); no cross-lane combine.  A copy that has not
+// landed after TMA_WAIT_NS sets PHCU_ST_TIMEOUT and ends the block.
+constexpr int ROWS_PER_TILE = 256;
+constexpr int ROWS_MAX_BYTES = 384;  // row length limit: two 96 KiB stages
+
+template <typename T, int KIND>
+__global__ void __launch_bounds__(ROWS_PER_TILE, 1) reduce_rows_kernel(const __grid_constant__ RedArgs a) {
+  static_assert(sizeof(T) == 4, "4-byte elements");
+  constexpr int VN = 4;
+  extern __shared__ __align__(128) unsigned char rows_smem[];
+  __shared__ __align__(8) uint64_t bars[2];
+  const int K = (int)a.K;
+  const int NV = K / VN;
+  const uint32_t row_bytes = (uint32_t)K * sizeof(T);
+  const uint32_t stage_bytes = ROWS_PER_TILE * row_bytes;
+  const uint32_t sb = (uint32_t)__cvta_generic_to_shared(rows_smem);
+  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&bars[0]);
+  const int64_t ntiles = (a.O + ROWS_PER_TILE - 1) / ROWS_PER_TILE;
+  const int64_t g = gridDim.x;
+  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
+  auto issue = [&](int64_t tile, int stg) {
+    const int64_t r0 = tile * ROWS_PER_TILE;
+    const uint32_t bytes = (uint32_t)min((int64_t)ROWS_PER_TILE, a.O - r0) * row_bytes;
+    mbar_expect_tx(bar0 + 8u * stg, bytes);
+    bulk_load_1d(sb + stg * stage_bytes, a.in + r0 * row_bytes, bytes, bar0 + 8u * stg);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar0 + 8, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  uint32_t st = 0;
+  int64_t t = blockIdx.x;
+  if (threadIdx.x == 0) {
+    if (t < ntiles) issue(t, 0);
+    if (t + g < ntiles) issue(t + g, 1);
+  }
+  const int r = threadIdx.x;
+  for (uint32_t i = 0; t < ntiles; i++, t += g) {
+    const int stg = i & 1;
+    const bool ok = mbar_wait_bounded(bar0 + 8u * stg, (i >> 1) & 1u, TMA_WAIT_NS);
+    if (!__syncthreads_and(ok)) {
+      st |= PHCU_ST_TIMEOUT;
+      if (threadIdx.x == 0 && t + g < ntiles) mbar_wait_bounded(bar0 + 8u * (stg ^ 1), ((i + 1) >> 1) & 1u, TMA_WAIT_NS);
+      break;
+    }
+    const int64_t o = t * ROWS_PER_TILE + r;
+    if (o < a.O) {
+      const unsigned char* row = rows_smem + stg * stage_bytes + (size_t)r * row_bytes;
+      const uint4* rv = reinterpret_cast<const uint4*>(row);
+      int q = r % NV;  // first vector read by this thread
+      if (KIND == RK_SUM) {
+        SumAcc<T> acc;
+        acc.init();
+        for (int j = 0; j < NV; j++) {
+          const uint4 u = rv[q];
+          acc.add(word32_as<T>(u.x));
+          acc.add(word32_as<T>(u.y));
+          acc.add(word32_as<T>(u.z));
+          acc.add(word32_as<T>(u.w));
+          q = (q + 1 == NV) ? 0 : q + 1;
+        }
+        if constexpr (std::is_same<T, float>::value) store_final(a, o, acc.value(), 0, false, 0, 0, st);
+        else store_final(a, o, 0, 0, true, (long long)acc.s, 0, st);
+      } else {
+        // the extreme value over the non-NaN elements, then its first index
+        T m = word32_as<T>(rv[0].x);
+        for (int j = 0; j < NV; j++) {
+          const uint4 u = rv[q];
+          m = Lim<T>::ext(m, word32_as<T>(u.x), is_max);
+          m = Lim<T>::ext(m, word32_as<T>(u.y), is_max);
+          m = Lim<T>::ext(m, word32_as<T>(u.z), is_max);
+          m = Lim<T>::ext(m, word32_as<T>(u.w), is_max);
+          q = (q + 1 == NV) ? 0 : q + 1;
+        }
+        int best = K;
+        for (int j = 0; j < NV; j++) {
+          const uint4 u = rv[q];
+          const int k0 = q * VN;
+          best = min(best, word32_as<T>(u.x) == m ? k0 : K);
+          best = min(best, word32_as<T>(u.y) == m ? k0 + 1 : K);
+          best = min(best, word32_as<T>(u.z) == m ? k0 + 2 : K);
+          best = min(best, word32_as<T>(u.w) == m ? k0 + 3 : K);
+          q = (q + 1 == NV) ? 0 : q + 1;
+        }
+        const T* re = reinterpret_cast<const T*>(row);
+        // a NaN first element (or no candidate) wins: the scan never moves off element 0
+        if (best == K || Lim<T>::nan(re[0])) best = 0;
+        const T v = re[best];  // the element itself (the sign of a zero)
+        double d;
+        long long l;
+        ext_parts<T>(v, d, l);
+        store_final(a, o, d, l, false, 0, best, st);
+      }
+    }
+    __syncthreads();  // every thread is done with this stage
+    if (threadIdx.x == 0 && t + 2 * g < ntiles) {
+      fence_proxy_async();
+      issue(t + 2 * g, stg);
+    }
+  }
+  if (st) atomicOr(a.status, st);
+}
+
+// Whether the staged row reduction applies: one contiguous reduced axis of
+// 32-96 four-byte elements (whole 16-byte vectors), rows back to back from a
+// 16-byte aligned start, no split, enough rows for every SM.
+static bool rows_fit(const RedArgs& a, const RedShape& sh) {
+  const int es = dtype_size(a.dtype);
+  return sh.mode == 0 && es == 4 && a.S == 1 && a.krank == 1 && a.kinner == 1 && a.orank == 1 &&
+         a.ostride[0] == a.K && a.K >= 32 && a.K * es <= ROWS_MAX_BYTES && (a.K * es) % 16 == 0 &&
+         ((uintptr_t)a.in % 16) == 0 && a.O >= (int64_t)ROWS_PER_TILE * ctx().sm_count;
+}
+
+template <typename T, int KIND>
+static int32_t launch_rows(const RedArgs& a) {
+  const size_t smem = 2 * (size_t)ROWS_PER_TILE * (size_t)a.K * sizeof(T);
+  const int per_sm = blocks_per_sm((const void*)reduce_rows_kernel<T, KIND>, ROWS_PER_TILE, smem);
+  const int64_t ntiles = (a.O + ROWS_PER_TILE - 1) / ROWS_PER_TILE;
+  const int64_t grid = std::min<int64_t>(ntiles, (int64_t)ctx().sm_count * per_sm);
+  reduce_rows_kernel<T, KIND><<<(unsigned)grid, ROWS_PER_TILE, smem, ctx().stream>>>(a);
+  count_launch();
+  return check_launch("reduce_rows_kernel");
+}
+
+static int32_t launch_rows_any(const RedArgs& a) {
+  const bool sum = a.op == PHCU_RED_SUM;
+  if (a.dtype == PHCU_F32) return sum ? launch_rows<float, RK_SUM>(a) : launch_rows<float, RK_EXT>(a);
+  return sum ? launch_rows<int32_t, RK_SUM>(a) : launch_rows<int32_t, RK_EXT>(a);
+}
+
+// Whether the one-launch full reduction applies: one contiguous reduced run,
+// 16-byte aligned, long enough to need many blocks.
+static bool full_run(const RedArgs& a, const RedShape& sh) {
+  return a.O == 1 && a.krank == 1 && a.kinner == 1 && sh.vec && a.K >= (int64_t)1 << 16 &&
+         ((uintptr_t)a.in % 16) == 0;
+}
+
+template <typename T, int KIND>
+static int32_t launch_all(const RedArgs& a, unsigned* arrive) {
+  reduce_all_kernel<T, KIND><<<(unsigned)a.S, 256, 0, ctx().stream>>>(a, arrive);
+  count_launch();
+  return check_launch("reduce_all_kernel");
+}
+
+// Blocks of a one-launch full reduction: four per SM, at most one per 4096
+// vectors (so every block has work for each of its threads).
+static int64_t full_run_blocks(const RedArgs& a) {
+  const int64_t want = (a.K / (16 / dtype_size(a.dtype)) + 4095) / 4096;
+  return std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx().sm_count * 4, want));
+}
+
+static int32_t launch_full_run(const RedArgs& a, unsigned* arrive) {
+  const bool sum = a.op == PHCU_RED_SUM;
+  switch (a.dtype) {
+    case PHCU_F32: return sum ? launch_all<float, RK_SUM>(a, arrive) : launch_all<float, RK_EXT>(a, arrive);
+    case PHCU_F64: return sum ? launch_all<double, RK_SUM>(a, arrive) : launch_all<double, RK_EXT>(a, arrive);
+    case PHCU_I32: return sum ? launch_all<int32_t, RK_SUM>(a, arrive) : launch_all<int32_t, RK_EXT>(a, arrive);
+    default: return sum ? launch_all<long long, RK_SUM>(a, arrive) : launch_all<long long, RK_EXT>(a, arrive);
+  }
+}
+
 template <typename T, int KIND>
 static int32_t launch_typed(const RedArgs& a, const RedShape& sh) {
   Context& c = ctx();
@@ -179,6 +446,7 @@ static int32_t launch_typed(const RedArgs& a, const RedShape& sh) {
 }
 
 static int32_t launch_reduce(const RedArgs& a, const RedShape& sh) {
+  if (rows_fit(a, sh)) return launch_rows_any(a);
   const bool sum = a.op == PHCU_RED_SUM;
   switch (a.dtype) {
     case PHCU_F32: return sum ? launch_typed<float, RK_SUM>(a, sh) : launch_typed<float, RK_EXT>(a, sh);
@@ -386,6 +654,27 @@ int32_t reduce_impl(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_
     return phcu_fill(out, &z);
   }
   void* scratch = nullptr;
+  if (full_run(a, sh)) {
+    // S block partials and the arrival counter (zeroed here, reset by the last block)
+    a.S = full_run_blocks(a);
+    a.chunk = a.K;
+    const size_t need = (size_t)a.S + 1;
+    if (partial_buf) {
+      if (need > partial_cap)
+        return fail(PHCU_ERR_UNSUPPORTED,
+                    "reduction needs %zu partials but the allocation-free scratch holds %zu; use phcu_reduce", need,
+                    partial_cap);
+      a.partial = (Partial*)partial_buf;
+    } else {
+      PHCU_TRY(scratch_alloc(need * sizeof(Partial), &scratch));
+      a.partial = (Partial*)scratch;
+    }
+    unsigned* arrive = (unsigned*)(a.partial + a.S);
+    cudaError_t e = cudaMemsetAsync(arrive, 0, sizeof(unsigned), ctx().stream);
+    int32_t rc = e == cudaSuccess ? launch_full_run(a, arrive) : cuda_fail(e, "cudaMemsetAsync(reduction counter)");
+    if (scratch) scratch_free(scratch);
+    return rc;
+  }
   if (a.S > 1) {
     size_t need = (size_t)a.S * (size_t)a.O;
     if (partial_buf) {

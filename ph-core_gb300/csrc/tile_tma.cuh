@@ -16,12 +16,13 @@
 
 #include <cuda.h>
 
+#include "async_copy.cuh"
+
 namespace phcu {
 
 constexpr uint32_t TMA_BOX_R = 32;                        // 4-byte elements per 128-byte box row
 constexpr uint32_t TMA_BOX_BYTES = TILE * 128;            // 64 W rows of 128 bytes
 constexpr uint32_t TMA_TILE_BYTES = 2 * TMA_BOX_BYTES;    // one staged input's 64x64 tile
-constexpr uint64_t TMA_WAIT_NS = 1000000000ull;           // give up on a copy after 1 s
 
 // Tensor maps of the staged inputs, in staging order (bit order of plan.staged).
 struct TmaMaps {
@@ -36,41 +37,6 @@ struct EvalTmaArgs {  // 64-byte aligned through CUtensorMap
   TmaMaps maps;
   EvalArgs a;
 };
-
-__device__ __forceinline__ uint64_t tma_now_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-// try_wait suspends the thread for up to the hinted 2 us while the phase is
-// incomplete, so waiting warps do not spin on the issue slots.
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity), "r"(2000u)
-      : "memory");
-  return ok != 0;
-}
-// Waits for the phase with the given parity to complete; false after limit_ns.
-static __device__ __noinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = tma_now_ns();
-  for (;;) {
-    for (int i = 0; i < 32; i++)
-      if (mbar_try_wait(bar, parity)) return true;
-    if (tma_now_ns() - t0 > limit_ns) return false;
-  }
-}
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // One box of a tensor map into shared memory, completing on bar.
 __device__ __forceinline__ void tma_load_box(const CUtensorMap* map, uint32_t dst, uint32_t bar, int ndim,
