@@ -357,9 +357,9 @@ PHCU_API int32_t phcu_tune_n_configs(int32_t* n);
 PHCU_API int32_t phcu_tune_features(const phcu_task_t* task, int32_t config, float* features);
 /* Times `task` under every config (reps each, median); ms[n_configs].  The
  * task runs as a batch of copies that fills the GPU (up to 512, about 2^22
- * elements in all), and ms is the time per copy: its cost inside a large
- * batch.  The task runs (reps + 1) x copies times per config, so an in-place
- * task changes its data. */
+ * elements in all), each copy writing its own scratch output of the task's
+ * shape, and ms is the time per copy: its cost inside a large batch.  The
+ * task's own output is not written. */
 PHCU_API int32_t phcu_tune_measure(const phcu_task_t* task, const phcu_program_t* programs, int32_t reps,
                           float* ms);
 /* Runs `task` once under `config` (standalone kernels). */

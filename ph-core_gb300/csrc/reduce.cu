@@ -591,9 +591,13 @@ int32_t plan_reduce(int32_t op, const phcu_view_t* in, int32_t axis, const phcu_
 
   const int64_t inner_out_stride = orank > 0 ? ost[orank - 1] : 0;
   const bool k_contig = (kst[krank - 1] == 1 || kst[krank - 1] == -1);
+  const int64_t ao = inner_out_stride < 0 ? -inner_out_stride : inner_out_stride;
+  const int64_t ak = kst[krank - 1] < 0 ? -kst[krank - 1] : kst[krank - 1];
   int mode, G = 32;
-  if (orank > 0 && (inner_out_stride == 1 || inner_out_stride == -1) && !(k_contig && O < target / 8)) {
+  if (orank > 0 && ao == 1 && !(k_contig && O < target / 8)) {
     mode = 1;
+  } else if (orank > 0 && !k_contig && ao < ak && O >= target / 8) {
+    mode = 1;  // neither axis contiguous: neighbouring threads read closer along the outputs
   } else {
     mode = 0;
   }

@@ -250,14 +250,30 @@ int32_t phcu_tune_measure(const phcu_task_t* task, const phcu_program_t* program
   // the time is divided by R: a task's cost inside a large batch (its work
   // items interleave with everyone else's) is its share of the throughput,
   // not the latency of a launch that it has to itself.
+  // Each copy writes its own contiguous output (scratch of the output's
+  // shape), as the tasks of a real batch do: copies sharing one output would
+  // turn every store into an L2 hit.
   const phcu_view_t& src = (task->kind == PHCU_TASK_EVAL && task->n_inputs == 0) ? task->out : task->in[0];
   const int64_t n = std::max<int64_t>(1, view_size(&src));
   const int R = (int)std::min<int64_t>(512, std::max<int64_t>(1, ((int64_t)1 << 22) / n));
-  int32_t rc = PHCU_OK;
+  const int64_t out_n = std::max<int64_t>(1, view_size(&task->out));
+  const size_t out_bytes = ((size_t)out_n * dtype_size(task->out.dtype) + 255) & ~(size_t)255;
+  void* outs = nullptr;
+  int32_t rc = scratch_alloc(out_bytes * R, &outs);
   for (int c = 0; c < NCONF && rc == PHCU_OK; c++) {
     phcu_task_t t = *task;
     apply_config(&t, c);
     std::vector<phcu_task_t> copies((size_t)R, t);
+    for (int k = 0; k < R; k++) {
+      phcu_view_t& o = copies[(size_t)k].out;
+      o.base = (char*)outs + (size_t)k * out_bytes;
+      o.offset = 0;
+      int64_t st = 1;
+      for (int i = o.rank - 1; i >= 0; i--) {
+        o.stride[i] = st;
+        st *= o.shape[i];
+      }
+    }
     void* b = nullptr;
     rc = phcu_batch_prepare(copies.data(), R, programs, nprog, &b);
     if (rc != PHCU_OK) break;
@@ -278,6 +294,7 @@ int32_t phcu_tune_measure(const phcu_task_t* task, const phcu_program_t* program
       ms[c] = v[v.size() / 2] / (float)R;
     }
   }
+  scratch_free(outs);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return rc;
