@@ -148,7 +148,9 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
     BTask bt;
     memset(&bt, 0, sizeof(bt));
     bt.h.counter = -1;
-    const int64_t chunk = t.chunk > 0 ? t.chunk : DEFAULT_CHUNK;
+    // elements per work item, within [2^10, 2^16]: one item is one block's
+    // work, and a much larger one would leave that block last in the launch
+    const int64_t chunk = std::min<int64_t>(std::max<int64_t>(t.chunk > 0 ? t.chunk : DEFAULT_CHUNK, 1 << 10), 1 << 16);
     if (t.kind == PHCU_TASK_EVAL) {
       if (t.prog < 0 || t.prog >= nprog)
         return fail_batch(fail(PHCU_ERR_INVALID, "batch task %d: program %d out of range", i, t.prog));

@@ -226,25 +226,29 @@ int32_t make_plan(const phcu_view_t* out, const phcu_view_t* const* ins, int nin
   uint32_t staged = 0;
   // index operands are computed by the ROW body only
   if (!any_index && r >= 2 && p->out.stride[W] == 1 && m[W].n >= 8) {
-    // candidate inputs: contiguous along some other axis R, far apart along W
+    // candidate inputs: contiguous along some other axis R (or stepping 2-4
+    // elements along it, a strided view of a permuted array) and far apart
+    // along W: read along R into shared memory, sectors are shared by
+    // neighbouring lanes, read along W every lane needs its own sector
+    auto stage = [](int64_t sa, int64_t sw) {
+      sa = sa < 0 ? -sa : sa;
+      sw = sw < 0 ? -sw : sw;
+      return (sa == 1 && sw > 2) || (sa >= 2 && sa <= 4 && sw >= 4 * sa);
+    };
     int best = -1;
     int64_t best_bytes = 0;
     for (int a = 0; a < W; a++) {
       if (m[a].n < 8) continue;
       int64_t bytes = 0;
-      for (int k = 0; k < nin; k++) {
-        int64_t sw = p->in[k].stride[W], sa = p->in[k].stride[a];
-        if ((sa == 1 || sa == -1) && (sw > 2 || sw < -2)) bytes += dtype_size(p->in[k].dtype);
-      }
+      for (int k = 0; k < nin; k++)
+        if (stage(p->in[k].stride[a], p->in[k].stride[W])) bytes += dtype_size(p->in[k].dtype);
       if (bytes > best_bytes) { best_bytes = bytes; best = a; }
     }
     if (best >= 0) {
       mode = MODE_TILE;
       raxis = best;
-      for (int k = 0; k < nin; k++) {
-        int64_t sw = p->in[k].stride[W], sa = p->in[k].stride[best];
-        if ((sa == 1 || sa == -1) && (sw > 2 || sw < -2)) staged |= 1u << k;
-      }
+      for (int k = 0; k < nin; k++)
+        if (stage(p->in[k].stride[best], p->in[k].stride[W])) staged |= 1u << k;
     }
   }
   if (force_mode == MODE_ROW) mode = MODE_ROW;

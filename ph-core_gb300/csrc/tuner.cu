@@ -1,8 +1,8 @@
 // tuner.cu -- launch-configuration autotuner and the learned (MLP) tuner.
 //
 // A configuration of a task is (work-item size, layout): the number of
-// elements one block takes from the work queue per item (2^11, 2^13, 2^15 or
-// 2^17) and whether the planner's launch shape or the alternative is used
+// elements one block takes from the work queue per item (2^12, 2^13, 2^14 or
+// 2^15) and whether the planner's launch shape or the alternative is used
 // (ROW vs TILE for elementwise programs, GROUP vs COLUMN for reductions).
 // phcu_tune_measure times a task alone under every configuration (exhaustive
 // autotune); the MLP (24 -> 64 -> 64 -> 1, ReLU, predicts log2 of the time)
@@ -25,7 +25,7 @@
 namespace phcu {
 
 constexpr int NCONF = 8;
-static const int32_t kChunk[4] = {1 << 11, 1 << 13, 1 << 15, 1 << 17};
+static const int32_t kChunk[4] = {1 << 12, 1 << 13, 1 << 14, 1 << 15};
 
 static void apply_config(phcu_task_t* t, int c) {
   t->chunk = kChunk[c % 4];

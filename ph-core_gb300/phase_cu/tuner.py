@@ -15,8 +15,8 @@ import numpy as np
 from . import _abi as A
 from .narray import _Buffer, init, lib
 
-DEFAULT_CONFIG = 1  # 8192-element work items, planner's launch shape
-CHUNKS = (2048, 8192, 32768, 131072)  # work-item sizes (elements) of configurations c % 4
+DEFAULT_CONFIG = 2  # 16384-element work items (the executor's default), planner's launch shape
+CHUNKS = (4096, 8192, 16384, 32768)  # work-item sizes (elements) of configurations c % 4
 
 
 def config_args(picks):

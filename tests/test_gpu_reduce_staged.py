@@ -86,3 +86,35 @@ def test_full_run(cu, ora, dt, n):
         assert abs(X.sum() - ref) <= 1e-6 * mag  # tolerance: 1e-6 of the sum of magnitudes
     # twice in a row: the arrival counter is reset by the launch that used it
     assert X.argmax() == [ora.reduce(ora.RED_ARGMAX, x)]
+
+
+# COLUMN layouts over contiguous arrays that the staged kernel takes (kept
+# outputs in runs of 64 whose reduced positions lie back to back, axis 2 of
+# [38, 64, 40, 64]; runs of 4096, axis 1 of [40, 33, 4096]; one run, axis 0 of
+# [37, 262144] and [9, 155648]; at least one 1024-output tile per SM)
+@pytest.mark.parametrize("dt", [np.float32, np.int32])
+@pytest.mark.parametrize("shape,axis", [([38, 64, 40, 64], 2), ([40, 33, 4096], 1), ([37, 262144], 0),
+                                        ([9, 152 * 1024], 0)])
+def test_staged_columns(cu, ora, dt, shape, axis):
+    rng = np.random.default_rng(sum(shape))
+    if np.issubdtype(dt, np.integer):
+        x = rng.integers(-60, 60, shape).astype(dt)
+    else:
+        x = (rng.standard_normal(shape) * 10).astype(dt)
+        flat = x.reshape(-1)
+        flat[::89] = 3.0
+        flat[11::997] = np.nan
+    X = cu.CuNArray.from_numpy(x)
+    oi = ora.I32
+    assert np.array_equal(X.argmax(axis=axis).to_narr(), ora.reduce(ora.RED_ARGMAX, x, axis, oi))
+    assert np.array_equal(X.argmin(axis=axis).to_narr(), ora.reduce(ora.RED_ARGMIN, x, axis, oi))
+    mx = X.max(axis=axis).to_narr()
+    assert np.array_equal(mx.view(np.uint32), ora.reduce(ora.RED_MAX, x, axis).view(np.uint32))
+    s = X.sum(axis=axis).to_narr()
+    if dt == np.int32:
+        assert np.array_equal(s, ora.reduce(ora.RED_SUM, x, axis))
+    else:
+        ref, mag = ora.reduce_f64(x, axis), ora.reduce_f64(np.abs(x), axis)
+        fin = np.isfinite(ref)
+        assert np.all(np.abs(s[fin] - ref[fin]) <= 1e-6 * mag[fin] + 1e-30)  # 1e-6 of the sum of magnitudes
+        assert np.all(np.isnan(s[~fin]))
