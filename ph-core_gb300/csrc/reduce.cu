@@ -341,180 +341,6 @@ static int32_t launch_rows_any(const RedArgs& a) {
   return sum ? launch_rows<int32_t, RK_SUM>(a) : launch_rows<int32_t, RK_EXT>(a);
 }
 
-// --------------------------------------------- columns staged by bulk copies
-// COLUMN reductions whose kept outputs form contiguous runs of L outputs and
-// whose reduced axis steps over whole rows of memory (4-byte elements,
-// 16-byte aligned): the innermost kept axes of a contiguous array.  A tile is
-// 1024 consecutive outputs in NR = 1024 / T rows of T = min(L, 1024) outputs;
-// a stage holds COL_P consecutive reduced positions of the tile's rows,
-// fetched by bulk copies (one per row when a row's positions lie back to back,
-// T == the position stride, else one per row and position) into a
-// three-stage ring; thread t owns four consecutive outputs of one row and
-// folds the positions of every stage in increasing order from shared memory
-// (consecutive threads read consecutive 16-byte words: no bank conflicts).
-// Copies of the next stages are in flight while a stage is folded, so the
-// DRAM sees long sequential runs instead of one 16-byte stream per thread.
-// A copy that has not landed after TMA_WAIT_NS sets PHCU_ST_TIMEOUT.
-constexpr int COL_THREADS = 256;
-constexpr int COL_TILE = 4 * COL_THREADS;  // outputs per tile
-constexpr int COL_P = 8;                   // reduced positions per stage
-constexpr int COL_STAGES = 3;
-
-struct ColGeom {
-  int64_t T;        // outputs per row of a tile
-  int64_t L;        // outputs per contiguous run
-  int64_t runs;     // number of runs
-  int64_t rstride;  // element stride between runs (0 with one run)
-  int64_t kst;      // element stride between reduced positions
-};
-
-template <typename T, int KIND>
-__global__ void __launch_bounds__(COL_THREADS) reduce_cols_kernel(const __grid_constant__ RedArgs a,
-                                                                   const ColGeom g) {
-  static_assert(sizeof(T) == 4, "4-byte elements");
-  extern __shared__ __align__(128) unsigned char col_smem[];
-  __shared__ __align__(8) uint64_t bars[COL_STAGES];
-  constexpr uint32_t STAGE_BYTES = (uint32_t)COL_TILE * COL_P * sizeof(T);
-  const uint32_t sb = (uint32_t)__cvta_generic_to_shared(col_smem);
-  const uint32_t bar0 = (uint32_t)__cvta_generic_to_shared(&bars[0]);
-  const int64_t NR = COL_TILE / g.T;                 // rows per tile
-  const int64_t tiles_per_run = g.L / g.T;
-  const int64_t ntiles = g.runs * tiles_per_run / NR;  // whole tiles only (the host checks divisibility)
-  const int64_t nsteps = (a.K + COL_P - 1) / COL_P;    // stages per tile
-  const uint32_t row_bytes = (uint32_t)(g.T * sizeof(T));
-  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
-  // element offset of row r (0..NR-1) of tile t
-  auto row_off = [&](int64_t t, int64_t r) {
-    const int64_t q = t * NR + r;  // global row index
-    return (q / tiles_per_run) * g.rstride + (q % tiles_per_run) * g.T;
-  };
-  // issues stage j (tile tj, positions [kp, kp + np)) into ring slot s
-  auto issue = [&](int64_t tj, int64_t kp, int s) {
-    const int np = (int)min((int64_t)COL_P, a.K - kp);
-    const uint32_t bar = bar0 + 8u * s;
-    mbar_expect_tx(bar, (uint32_t)(NR * np) * row_bytes);
-    for (int64_t r = 0; r < NR; r++) {
-      const char* src = a.in + (row_off(tj, r) + kp * g.kst) * (int64_t)sizeof(T);
-      const uint32_t dst = sb + s * STAGE_BYTES + (uint32_t)(r * COL_P) * row_bytes;
-      if (g.kst == g.T) {
-        bulk_load_1d(dst, src, (uint32_t)np * row_bytes, bar);
-      } else {
-        for (int j = 0; j < np; j++) bulk_load_1d(dst + j * row_bytes, src + j * g.kst * (int64_t)sizeof(T), row_bytes, bar);
-      }
-    }
-  };
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < COL_STAGES; s++) mbar_init(bar0 + 8u * s, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  // the block's work: stages j = 0.. of its tiles t = blockIdx.x + i * gridDim.x
-  const int64_t my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  const int64_t total = my_tiles * nsteps;
-  auto stage_tile = [&](int64_t j) { return blockIdx.x + (j / nsteps) * (int64_t)gridDim.x; };
-  if (threadIdx.x == 0)
-    for (int s = 0; s < COL_STAGES && s < total; s++) issue(stage_tile(s), (s % nsteps) * COL_P, s);
-  const int r = (int)(threadIdx.x / (g.T / 4));  // this thread's row of the tile
-  const int v = (int)(threadIdx.x % (g.T / 4));  // its 16-byte word in the row
-  uint32_t st = 0;
-  SumAcc<T> sacc[4];
-  ExtAcc<T> eacc[4];
-  for (int64_t j = 0; j < total; j++) {
-    const int s = (int)(j % COL_STAGES);
-    const int64_t kp = (j % nsteps) * COL_P;
-    if (kp == 0) {
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        sacc[e].init();
-        eacc[e].init();
-      }
-    }
-    const bool ok = mbar_wait_bounded(bar0 + 8u * s, (uint32_t)((j / COL_STAGES) & 1), TMA_WAIT_NS);
-    if (!__syncthreads_and(ok)) {
-      st |= PHCU_ST_TIMEOUT;
-      if (threadIdx.x == 0)  // the other stages' copies in flight, bounded
-        for (int64_t q = j + 1; q < j + COL_STAGES && q < total; q++)
-          mbar_wait_bounded(bar0 + 8u * (q % COL_STAGES), (uint32_t)((q / COL_STAGES) & 1), TMA_WAIT_NS);
-      break;
-    }
-    const int np = (int)min((int64_t)COL_P, a.K - kp);
-    const unsigned char* base = col_smem + s * STAGE_BYTES + (size_t)(r * COL_P) * row_bytes + (size_t)v * 16;
-    for (int p = 0; p < np; p++) {
-      const uint4 u = *reinterpret_cast<const uint4*>(base + (size_t)p * row_bytes);
-      const T x[4] = {word32_as<T>(u.x), word32_as<T>(u.y), word32_as<T>(u.z), word32_as<T>(u.w)};
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        if (KIND == RK_SUM) sacc[e].add(x[e]);
-        else eacc[e].add(x[e], kp + p, is_max);
-      }
-    }
-    if (kp + COL_P >= a.K) {  // the tile's last stage: store its outputs
-      const int64_t t = stage_tile(j);
-      const int64_t q = t * NR + r;
-      const int64_t o0 = (q / tiles_per_run) * g.L + (q % tiles_per_run) * g.T + (int64_t)v * 4;
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        if (KIND == RK_SUM) {
-          if constexpr (std::is_same<T, float>::value) store_final(a, o0 + e, sacc[e].value(), 0, false, 0, 0, st);
-          else store_final(a, o0 + e, 0, 0, true, (long long)sacc[e].s, 0, st);
-        } else {
-          long long idx = eacc[e].i;
-          T val = eacc[e].v;
-          const T first = *reinterpret_cast<const T*>(a.in + (row_off(t, r) + (int64_t)v * 4 + e) * (int64_t)sizeof(T));
-          if (idx < 0 || Lim<T>::nan(first)) {
-            idx = 0;
-            val = first;
-          }
-          double d;
-          long long l;
-          ext_parts<T>(val, d, l);
-          store_final(a, o0 + e, d, l, false, 0, idx, st);
-        }
-      }
-    }
-    __syncthreads();  // every thread is done with slot s
-    if (threadIdx.x == 0 && j + COL_STAGES < total) {
-      fence_proxy_async();
-      issue(stage_tile(j + COL_STAGES), ((j + COL_STAGES) % nsteps) * COL_P, s);
-    }
-  }
-  if (st) atomicOr(a.status, st);
-}
-
-// Geometry of a COLUMN reduction the staged kernel takes, or false.
-static bool cols_fit(const RedArgs& a, const RedShape& sh, ColGeom* g) {
-  const int es = dtype_size(a.dtype);
-  if (!(sh.mode == 1 && sh.vec && es == 4 && a.S == 1 && a.krank == 1 && a.kstride[0] > 0)) return false;
-  if (a.orank < 1 || a.orank > 2 || a.ostride[a.orank - 1] != 1) return false;
-  g->L = a.oshape[a.orank - 1];
-  g->runs = a.orank == 2 ? a.oshape[0] : 1;
-  g->rstride = a.orank == 2 ? a.ostride[0] : 0;
-  g->kst = a.kstride[0];
-  g->T = g->L >= COL_TILE ? COL_TILE : g->L;
-  if (g->T < 32 || COL_TILE % g->T != 0 || g->L % g->T != 0) return false;
-  const int64_t rows = g->runs * (g->L / g->T);
-  if (rows % (COL_TILE / g->T) != 0) return false;
-  if (((uintptr_t)a.in % 16) != 0 || (g->kst * es) % 16 != 0 || (g->rstride * es) % 16 != 0) return false;
-  return rows / (COL_TILE / g->T) >= ctx().sm_count;  // a tile for every SM
-}
-
-template <typename T, int KIND>
-static int32_t launch_cols(const RedArgs& a, const ColGeom& g) {
-  const size_t smem = (size_t)COL_STAGES * COL_TILE * COL_P * sizeof(T);
-  const int per_sm = blocks_per_sm((const void*)reduce_cols_kernel<T, KIND>, COL_THREADS, smem);
-  const int64_t ntiles = g.runs * (g.L / g.T) / (COL_TILE / g.T);
-  const int64_t grid = std::min<int64_t>(ntiles, (int64_t)ctx().sm_count * per_sm);
-  reduce_cols_kernel<T, KIND><<<(unsigned)grid, COL_THREADS, smem, ctx().stream>>>(a, g);
-  count_launch();
-  return check_launch("reduce_cols_kernel");
-}
-
-static int32_t launch_cols_any(const RedArgs& a, const ColGeom& g) {
-  const bool sum = a.op == PHCU_RED_SUM;
-  if (a.dtype == PHCU_F32) return sum ? launch_cols<float, RK_SUM>(a, g) : launch_cols<float, RK_EXT>(a, g);
-  return sum ? launch_cols<int32_t, RK_SUM>(a, g) : launch_cols<int32_t, RK_EXT>(a, g);
-}
-
 // Whether the one-launch full reduction applies: one contiguous reduced run,
 // 16-byte aligned, long enough to need many blocks.
 static bool full_run(const RedArgs& a, const RedShape& sh) {
@@ -621,8 +447,6 @@ static int32_t launch_typed(const RedArgs& a, const RedShape& sh) {
 
 static int32_t launch_reduce(const RedArgs& a, const RedShape& sh) {
   if (rows_fit(a, sh)) return launch_rows_any(a);
-  ColGeom cg;
-  if (cols_fit(a, sh, &cg)) return launch_cols_any(a, cg);
   const bool sum = a.op == PHCU_RED_SUM;
   switch (a.dtype) {
     case PHCU_F32: return sum ? launch_typed<float, RK_SUM>(a, sh) : launch_typed<float, RK_EXT>(a, sh);

@@ -542,6 +542,9 @@ __device__ __forceinline__ void group_vec(const RedArgs& a, int64_t o0, int64_t 
 // kept axis has unit stride and a length divisible by VN), eight reduced
 // positions in flight (four: 2-7% slower on 64x128x128x64, axes 0-2).  Requires every output row start and every reduced
 // stride to be 16-byte aligned.
+#ifndef PHCU_COL_INFLIGHT
+#define PHCU_COL_INFLIGHT 8
+#endif
 template <typename T, int KIND>
 __device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t split, uint32_t& st) {
   constexpr int VN = 16 / sizeof(T);
@@ -560,12 +563,13 @@ __device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t
   if (a.krank == 1) {
     const int64_t ks = a.kinner * (int64_t)sizeof(T);
     const char* p = base + k0 * ks;
-    for (; k + 7 < k1; k += 8, p += 8 * ks) {
-      T x[8][VN];
+    constexpr int NF = PHCU_COL_INFLIGHT;
+    for (; k + NF - 1 < k1; k += NF, p += NF * ks) {
+      T x[NF][VN];
 #pragma unroll
-      for (int j = 0; j < 8; j++) ld16<T>(p + j * ks, x[j]);
+      for (int j = 0; j < NF; j++) ld16<T>(p + j * ks, x[j]);
 #pragma unroll
-      for (int j = 0; j < 8; j++)
+      for (int j = 0; j < NF; j++)
 #pragma unroll
         for (int e = 0; e < VN; e++) {
           if (KIND == RK_SUM) sacc[e].add(x[j][e]);
