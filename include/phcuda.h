@@ -318,9 +318,9 @@ typedef struct {
   int32_t axis;     /* reduce axis (REDUCE) */
   int32_t n_inputs; /* EVAL: 0..PHCU_MAX_INPUTS; REDUCE: 1 */
   int32_t prog;     /* index into the program table (EVAL) */
-  int32_t chunk;    /* elements per work item (0 = library default 16384; clamped to [1024, 65536]) */
-  int32_t layout;   /* 0 = planner's launch shape; 1 = the alternative (ROW for
-                       EVAL, the other of GROUP/COLUMN for REDUCE) */
+  int32_t chunk;    /* elements per work item (0 = library default 32768; clamped to [1024, 65536]) */
+  int32_t layout;   /* EVAL: 0 = planner's launch shape, 1 = ROW; a REDUCE task
+                       always takes the planner's layout */
   int32_t pad;
   phcu_view_t in[PHCU_MAX_INPUTS];
   phcu_view_t out;

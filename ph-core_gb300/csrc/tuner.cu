@@ -2,10 +2,10 @@
 //
 // A configuration of a task is (work-item size, layout): the number of
 // elements one block takes from the work queue per item (2^12, 2^13, 2^14 or
-// 2^15) and whether the planner's launch shape or the alternative is used
-// (ROW vs TILE for elementwise programs, GROUP vs COLUMN for reductions).
-// phcu_tune_measure times a task alone under every configuration (exhaustive
-// autotune); the MLP (24 -> 64 -> 64 -> 1, ReLU, predicts log2 of the time)
+// 2^15) and, for elementwise programs, whether the planner's launch shape or
+// ROW is used (a reduction keeps the planner's layout under both).
+// phcu_tune_measure times a task under every configuration (exhaustive
+// autotune) as its share of a batch of copies that fills the GPU; the MLP (24 -> 64 -> 64 -> 1, ReLU, predicts log2 of the time)
 // is trained on those timings by the kernels below and then ranks the
 // configurations of unseen tasks without timing them.
 //

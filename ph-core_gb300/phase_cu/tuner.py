@@ -15,7 +15,7 @@ import numpy as np
 from . import _abi as A
 from .narray import _Buffer, init, lib
 
-DEFAULT_CONFIG = 2  # 16384-element work items (the executor's default), planner's launch shape
+DEFAULT_CONFIG = 3  # 32768-element work items (the executor's default), planner's launch shape
 CHUNKS = (4096, 8192, 16384, 32768)  # work-item sizes (elements) of configurations c % 4
 
 
