@@ -230,19 +230,24 @@ def job_gbs(step_bytes, world, ms_per_step):
     return step_bytes * world / (ms_per_step * 1e-3) / 1e9
 
 
-TRAFFIC_FILE = os.path.join(ROOT, "profiles", "traffic_strided_views_512x512x256.json")
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# dominant class, binary + - * / on permuted 32-bit views, from one ncu capture
+# of four launches on a 256x512x256 case (half the bench's elements; reads and
+# writes both scale with the element count, so the figure is doubled):
+#   python bench.py --profile-class binary_permute --profile-shape 256x512x256 --steps 1 --warmup 0
+#   ncu --metrics gpu__time_duration.sum,dram__bytes_read.sum,dram__bytes_write.sum
+#       --clock-control none -k regex:eval -c 4 --csv --log-file traffic_permute.csv <same command>
+# Mean per launch there: 268,647,040 B read + 92,249,920 B written.
+MEASURED_TRAFFIC = {"binary_permute": 2 * (268647040 + 92249920)}
+TRAFFIC_SOURCE = ("ncu, 4 launches of eval_tma_kernel<u32,2> at 256x512x256, scaled x2 "
+                  "(profiles/eval_tma_kernel_traffic_binary_permute_256x512x256.md)")
 
 
 def measured_traffic(cls):
-    """DRAM bytes per launch of one operation class, from the committed ncu
-    launch-list summary (dram__bytes_read.sum + dram__bytes_write.sum); None
-    when no summary covers the class."""
-    try:
-        with open(TRAFFIC_FILE) as f:
-            t = json.load(f)
-        return t["classes"].get(cls), os.path.relpath(TRAFFIC_FILE, ROOT)
-    except (OSError, ValueError, KeyError):
-        return None, None
+    """DRAM bytes per full-size launch of one operation class from the ncu
+    capture; None when no capture covers the class."""
+    t = MEASURED_TRAFFIC.get(cls)
+    return t, (TRAFFIC_SOURCE if t is not None else None)
 
 
 def profile_config(args):

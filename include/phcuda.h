@@ -356,7 +356,7 @@ PHCU_API int32_t phcu_tune_n_configs(int32_t* n);
 /* Feature vector of (task, config) as the tuner sees it. */
 PHCU_API int32_t phcu_tune_features(const phcu_task_t* task, int32_t config, float* features);
 /* Times `task` under every config (reps each, median); ms[n_configs].  The
- * task runs as a batch of copies that fills the GPU (up to 512, about 2^22
+ * task runs as a batch of copies that fills the GPU (up to 512, about 2^25
  * elements in all), each copy writing its own scratch output of the task's
  * shape, and ms is the time per copy: its cost inside a large batch.  The
  * task's own output is not written. */

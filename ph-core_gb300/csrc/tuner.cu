@@ -255,7 +255,9 @@ int32_t phcu_tune_measure(const phcu_task_t* task, const phcu_program_t* program
   // turn every store into an L2 hit.
   const phcu_view_t& src = (task->kind == PHCU_TASK_EVAL && task->n_inputs == 0) ? task->out : task->in[0];
   const int64_t n = std::max<int64_t>(1, view_size(&src));
-  const int R = (int)std::min<int64_t>(512, std::max<int64_t>(1, ((int64_t)1 << 22) / n));
+  // 2^25 elements in all: even at the largest work items a batch of big
+  // copies has a few items for every block, as the tasks of a real batch do
+  const int R = (int)std::min<int64_t>(512, std::max<int64_t>(1, ((int64_t)1 << 25) / n));
   const int64_t out_n = std::max<int64_t>(1, view_size(&task->out));
   const size_t out_bytes = ((size_t)out_n * dtype_size(task->out.dtype) + 255) & ~(size_t)255;
   void* outs = nullptr;
