@@ -16,9 +16,10 @@ namespace phcu {
 constexpr int TILE_THREADS = 256;
 
 // FAST selects how the per-element work runs: the interpreter (FAST_NONE), a
-// plain move (FAST_COPY), an in-place binary operator (FAST_BINOP) or the
-// interpreter reduced to pre-decoded instructions (FAST_FX, program_is_fx).
-enum : int { FAST_NONE = 0, FAST_COPY = 1, FAST_BINOP = 2, FAST_FX = 3 };
+// plain move (FAST_COPY), an in-place binary operator (FAST_BINOP), the
+// interpreter reduced to pre-decoded instructions (FAST_FX, program_is_fx) or
+// Int32 / Int32 -> Float64 alone (FAST_IDIV, program_is_idiv; 64-bit slots).
+enum : int { FAST_NONE = 0, FAST_COPY = 1, FAST_BINOP = 2, FAST_FX = 3, FAST_IDIV = 4 };
 constexpr bool interpreted(int fast) { return fast == FAST_NONE || fast == FAST_FX; }
 
 // ----------------------------------------------------------------- ROW
@@ -96,6 +97,9 @@ __device__ __forceinline__ void row_group(const EvalPlan& p, const phcu_program_
     run_binop<S, V>(prog, in[0], in[1], st);
 #pragma unroll
     for (int v = 0; v < V; v++) acc[v] = in[0][v];
+  } else if constexpr (FAST == FAST_IDIV && NIN >= 2 && sizeof(S) == 8) {
+#pragma unroll
+    for (int v = 0; v < V; v++) acc[v] = int32_div_f64_bits(si32(in[0][v]), si32(in[1][v]));
   } else if constexpr (FAST == FAST_FX) {
     run_program_fx<S, NIN, V>(prog, in, acc, st);
   } else {
@@ -350,6 +354,9 @@ __device__ __forceinline__ void tile_body(const EvalPlan& p, const phcu_program_
       run_binop<S, V>(prog, in[0], in[1], st);
 #pragma unroll
       for (int v = 0; v < V; v++) acc[v] = in[0][v];
+    } else if constexpr (FAST == FAST_IDIV && NIN >= 2 && sizeof(S) == 8) {
+#pragma unroll
+      for (int v = 0; v < V; v++) acc[v] = int32_div_f64_bits(si32(in[0][v]), si32(in[1][v]));
     } else if constexpr (FAST == FAST_FX) {
       run_program_fx<S, NIN, V>(prog, in, acc, st);
     } else {
@@ -415,6 +422,13 @@ inline bool program_is_binop(const phcu_program_t& P, const EvalPlan& plan) {
   if (!int_exp && b.btype != b.type) return false;
   if (P.n_instr == 3 && P.code[2].op != PHCU_I_CVT) return false;
   return true;
+}
+
+// [ACC = IN0 (Int32); ACC = ACC / IN1 (Int32)] into a Float64 output: the
+// exact division alone, without the binary operator's run-time dispatch.
+inline bool program_is_idiv(const phcu_program_t& P, const EvalPlan& plan) {
+  return program_is_binop(P, plan) && P.n_instr == 2 && P.code[1].op == PHCU_OP_DIV && P.code[1].type == PHCU_I32 &&
+         plan.in[0].dtype == PHCU_I32 && plan.in[1].dtype == PHCU_I32 && plan.out.dtype == PHCU_F64;
 }
 
 inline bool program_is_copy(const phcu_program_t& P, const EvalPlan& plan) {

@@ -18,11 +18,11 @@ struct EvalArgs {
 
 constexpr int ROW_THREADS = 256;
 
-// Copies get four resident blocks per SM, everything else three: the kernels
-// are latency-bound when registers limit residency.
+// Copies and the Int32 division get four resident blocks per SM, everything
+// else three: the kernels are latency-bound when registers limit residency.
 template <int FAST>
 constexpr int min_blocks() {
-  return FAST == FAST_COPY ? 4 : 3;
+  return (FAST == FAST_COPY || FAST == FAST_IDIV) ? 4 : 3;
 }
 
 // ROW kernels of 32-bit in-place binary operators: 8 elements per thread at
@@ -150,6 +150,10 @@ int32_t launch_eval_sn(const EvalArgs& A) {
   if constexpr (NIN == 1) {
     if (program_is_copy(A.prog, A.plan))
       return tile ? launch_tile_any<S, NIN, false, FAST_COPY>(A) : launch_row<S, NIN, false, FAST_COPY>(A);
+  }
+  if constexpr (NIN == 2 && sizeof(S) == 8) {
+    if (program_is_idiv(A.prog, A.plan))
+      return tile ? launch_tile_any<S, NIN, false, FAST_IDIV>(A) : launch_row<S, NIN, false, FAST_IDIV>(A);
   }
   if constexpr (NIN == 2) {
     if (program_is_binop(A.prog, A.plan))

@@ -282,63 +282,53 @@ __device__ __forceinline__ F powi(F a, int32_t b) {
 // correctly rounded to nearest-even.  GB300's FP64 rate makes a double
 // division cost about as much as reading the operands many times over, so the
 // quotient is computed exactly with 32-bit integer long division instead
-// (schoolbook division with estimated digits, Knuth TAOCP vol. 2, 4.3.1):
-// normalise |x| and |y| so their quotient m lies in [1, 2) and the divisor b'
-// in [2^30, 2^31), then take three 18-bit digits of the fraction.  Each digit
-// is estimated as round(r * 2^18 / b') from the top 23 bits of the remainder
-// r and an FP32 reciprocal of b'; the estimate is within 0.15 of the exact
-// real quotient, so after rounding it is the true digit or one above it, and
-// a single check of the sign of the new remainder (which then fits an int32)
-// corrects it.  The 54 fraction bits and a sticky bit from the last remainder
-// are rounded to 52 bits and assembled into the double's bits.  Every
-// |quotient| of two non-zero Int32 lies in [2^-31, 2^31], so the result is
-// always normal.
+// (schoolbook division with estimated digits, Knuth TAOCP vol. 2, 4.3.1, in
+// the redundant signed-digit form of SRT division): normalise |x| and |y| so
+// both lie in [2^30, 2^31) (divisor b'), take the integer part of their
+// quotient m in [1, 2) and then three 18-bit fraction digits.  Each digit is
+// round(r * 2^18 / b') estimated from the top 22 bits of the signed remainder
+// r and an FP32 reciprocal of b' (within 0.19 of the exact real quotient), and
+// is never corrected: the new remainder r * 2^18 - q * b' lies in (-b', b'),
+// fits an int32, and the next digit absorbs its sign.  The fraction
+// F = d0 * 2^36 + d1 * 2^18 + d2 then satisfies m * 2^54 = 2^54 + F + r3 / b'.
+// No quotient of two Int32 lies exactly halfway between two doubles (an odd
+// number above 2^53 would have to divide |x| <= 2^31), so rounding to nearest is
+// (F + 2) >> 2, or (F + 1) >> 2 when r3 < 0.  Every |quotient| of two non-zero
+// Int32 lies in [2^-31, 2^31], so the result is always normal.
 __device__ __forceinline__ uint64_t int32_div_f64_bits(int32_t x, int32_t y) {
-  const uint64_t sign = (uint64_t)(((uint32_t)x ^ (uint32_t)y) >> 31) << 63;
   const uint32_t a = x < 0 ? 0u - (uint32_t)x : (uint32_t)x;
   const uint32_t b = y < 0 ? 0u - (uint32_t)y : (uint32_t)y;
-  if (b == 0) {
+  if (b == 0 || a == 0) {
+    if (b != 0) return (uint64_t)((uint32_t)y >> 31) << 63;                    // +0.0 / y = +-0.0
     if (a == 0) return 0x7ff8000000000000ull;                                  // 0 / 0 = NaN
-    return ((uint64_t)((uint32_t)x >> 31) << 63) | 0x7ff0000000000000ull;        // x / 0 = +-Inf (sign of x)
+    return ((uint64_t)((uint32_t)x >> 31) << 63) | 0x7ff0000000000000ull;      // x / 0 = +-Inf (sign of x)
   }
-  if (a == 0) return (uint64_t)((uint32_t)y >> 31) << 63;                        // +0.0 / y = +-0.0
-  const int la = 31 - __clz(a), lb = 31 - __clz(b);
-  // a' and b' with the leading one at bit 30 (|Int32| <= 2^31 leaves bit 0 of a << (31 - la) clear)
-  uint32_t an = (a << (31 - la)) >> 1;
-  const uint32_t bn = (b << (31 - lb)) >> 1;
-  int e = la - lb;
-  if (an < bn) {
-    an <<= 1;
-    e -= 1;
-  }
-  // m = an / bn in [1, 2): integer part 1, remainder r < bn < 2^31
-  uint32_t r = an - bn;
-  float rc;  // 2^26 / bn within 1.5 ulp: bn rounds to FP32 (0.5 ulp), rcp.approx adds at most 1 ulp
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rc) : "f"(__uint2float_rn(bn)));
-  rc *= 67108864.0f;
-  uint32_t dg[3];
+  const int za = __clz(a), zb = __clz(b);
+  // leading one at bit 30 (|Int32| <= 2^31 leaves bit 0 of a << za clear)
+  const uint32_t an = (a << za) >> 1, bn = (b << zb) >> 1;
+  const uint32_t c = an < bn;  // m = 2 an / bn, one binade lower
+  int32_t r = (int32_t)((an << c) - bn);
+  const int e = zb - za - (int)c;
+  // bn * 2^-27 in [8, 16) as an FP32 built from the top 24 bits of bn
+  // (truncated: within 1 ulp); rcp.approx adds at most 1 ulp, so rc is
+  // 2^27 / bn within 2 ulp and moves an estimate below 2^18 by under 1/16
+  float rc;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rc) : "f"(__uint_as_float(0x40800000u + (bn >> 7))));
+  int32_t d[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    // r >> 8 < 2^23 converts exactly through the 2^23 exponent; the dropped bits
-    // move the estimate by under 2^8 * 2^18 / 2^30 = 1/16
-    const float rh = __uint_as_float(0x4b000000u | (r >> 8)) - 8388608.0f;
-    // rounded to an integer by the 1.5 * 2^23 offset, read from the mantissa field
-    uint32_t q = __float_as_uint(__fmaf_rn(rh, rc, 12582912.0f)) & 0x3fffffu;
-    int32_t rem = (int32_t)((r << 18) - q * bn);  // exact: the true value lies in [-bn, bn)
-    if (rem < 0) {
-      q -= 1;
-      rem += (int32_t)bn;
-    }
-    dg[k] = q;
-    r = (uint32_t)rem;
+    // r >> 9 in [-2^22, 2^22) converts exactly through the 1.5 * 2^23 offset;
+    // the dropped bits move the estimate by under 2^9 * 2^18 / 2^30 = 1/8
+    const float rh = __int_as_float(0x4b400000 + (r >> 9)) - 12582912.0f;
+    // rounded to an integer by the same offset, read back from the bits
+    const int32_t q = __float_as_int(__fmaf_rn(rh, rc, 12582912.0f)) - 0x4b400000;
+    r = (int32_t)(((uint32_t)r << 18) - (uint32_t)q * bn);  // exact: the true value lies in (-bn, bn)
+    d[k] = q;
   }
-  // fraction bits f1..f54 = dg[0] dg[1] dg[2]; f53 is the guard bit, f54 and the remainder are sticky
-  uint64_t mant = ((uint64_t)dg[0] << 34) | ((uint64_t)dg[1] << 16) | (dg[2] >> 2);
-  const bool guard = (dg[2] >> 1) & 1u;
-  const bool sticky = (dg[2] & 1u) || r != 0;
-  mant += (guard && (sticky || (mant & 1u))) ? 1u : 0u;
-  // a carry out of the 52 mantissa bits (m rounded up to 2.0) moves into the exponent
-  return sign | (((uint64_t)(e + 1023) << 52) + mant);
+  const int64_t F = ((((int64_t)d[0] << 18) + d[1]) << 18) + d[2];
+  const uint64_t mant = (uint64_t)(F + 2 - (r < 0)) >> 2;
+  const uint64_t sign = (uint64_t)(((uint32_t)x ^ (uint32_t)y) & 0x80000000u) << 32;
+  return sign + ((uint64_t)(e + 1023) << 52) + mant;
 }
 
 // ------------------------------------------------- vector op kernels

@@ -539,12 +539,16 @@ __device__ __forceinline__ void group_vec(const RedArgs& a, int64_t o0, int64_t 
 
 // COLUMN with 16-byte loads across outputs: one thread reduces VN consecutive
 // outputs o0 .. o0 + VN - 1, which are consecutive in memory (the innermost
-// kept axis has unit stride and a length divisible by VN), eight reduced
-// positions in flight (four: 2-7% slower on 64x128x128x64, axes 0-2).  Requires every output row start and every reduced
-// stride to be 16-byte aligned.
-#ifndef PHCU_COL_INFLIGHT
-#define PHCU_COL_INFLIGHT 8
-#endif
+// kept axis has unit stride and a length divisible by VN).  Reduced positions
+// in flight: eight for extrema (four: 2-7% slower on 64x128x128x64, axes
+// 0-2), four for compensated floating-point sums, whose adds then interleave
+// with the next loads (a [64, 128, 8192] column sum: 49.3 -> 43.6 us; sixteen:
+// 51.4 us).  Requires every output row start and every reduced stride to be
+// 16-byte aligned.
+template <typename T, int KIND>
+constexpr int col_inflight() {
+  return (KIND == RK_SUM && (std::is_same<T, float>::value || std::is_same<T, double>::value)) ? 4 : 8;
+}
 template <typename T, int KIND>
 __device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t split, uint32_t& st) {
   constexpr int VN = 16 / sizeof(T);
@@ -563,29 +567,18 @@ __device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t
   if (a.krank == 1) {
     const int64_t ks = a.kinner * (int64_t)sizeof(T);
     const char* p = base + k0 * ks;
-    constexpr int NF = PHCU_COL_INFLIGHT;
+    constexpr int NF = col_inflight<T, KIND>();
     for (; k + NF - 1 < k1; k += NF, p += NF * ks) {
       T x[NF][VN];
 #pragma unroll
       for (int j = 0; j < NF; j++) ld16<T>(p + j * ks, x[j]);
-      if constexpr (KIND == RK_SUM && std::is_same<T, float>::value) {
-        // neighbouring positions are added in FP32 before the compensated
-        // add: each pair's rounding is at most 2^-24 of the pair, so the sum
-        // stays within 2^-24 of the sum of magnitudes, and the compensated
-        // adds (the ALU work of this loop) are halved
 #pragma unroll
-        for (int j = 0; j < NF; j += 2)
+      for (int j = 0; j < NF; j++)
 #pragma unroll
-          for (int e = 0; e < VN; e++) sacc[e].add(x[j][e] + x[j + 1][e]);
-      } else {
-#pragma unroll
-        for (int j = 0; j < NF; j++)
-#pragma unroll
-          for (int e = 0; e < VN; e++) {
-            if (KIND == RK_SUM) sacc[e].add(x[j][e]);
-            else eacc[e].add(x[j][e], k + j, is_max);
-          }
-      }
+        for (int e = 0; e < VN; e++) {
+          if (KIND == RK_SUM) sacc[e].add(x[j][e]);
+          else eacc[e].add(x[j][e], k + j, is_max);
+        }
     }
     for (; k < k1; k++, p += ks) {
       T x[VN];

@@ -191,6 +191,9 @@ __device__ __forceinline__ void tma_tile_body(const EvalPlan& p, const phcu_prog
       run_binop<S, V>(prog, in[0], in[1], st);
 #pragma unroll
       for (int v = 0; v < V; v++) acc[v] = in[0][v];
+    } else if constexpr (FAST == FAST_IDIV && NIN >= 2 && sizeof(S) == 8) {
+#pragma unroll
+      for (int v = 0; v < V; v++) acc[v] = int32_div_f64_bits(si32(in[0][v]), si32(in[1][v]));
     } else if constexpr (FAST == FAST_FX) {
       run_program_fx<S, NIN, V>(prog, in, acc, st);
     } else {

@@ -219,14 +219,14 @@ def test_fastdiv_formula():
             assert (t + n) >> l == n // d, (n, d)
 
 
-def _int32_div_f64_bits(x, y):
+def _int32_div_f64_bits(x, y, ulps=0):
     """Restatement of the device's exact Int32 / Int32 -> Float64 long division:
-    three 18-bit digits, each estimated in FP32 and corrected once by the sign
-    of the remainder.  The device's reciprocal is rcp.approx (within 1 ulp of
-    the correctly rounded one used here), so the mirror also checks that the
-    estimate stays within 0.25 of the exact digit quotient: a 1-ulp change of
-    the reciprocal moves it by under 0.05, which keeps the rounded estimate the
-    true digit or one above it."""
+    three 18-bit signed digits, each estimated in FP32 and never corrected, the
+    last remainder's sign folded into the rounding.  The divisor enters the
+    reciprocal truncated to 24 bits; the device's reciprocal is rcp.approx,
+    within 1 ulp of the correctly rounded one used here; `ulps`
+    moves the reciprocal by that many ulps, and every estimate must stay within
+    1/2 of the exact digit quotient (so the new remainder stays in (-b', b'))."""
     from fractions import Fraction
 
     sign = ((x < 0) ^ (y < 0)) << 63
@@ -235,28 +235,29 @@ def _int32_div_f64_bits(x, y):
         return 0x7FF8000000000000 if a == 0 else ((x < 0) << 63) | 0x7FF0000000000000
     if a == 0:
         return (y < 0) << 63
-    la, lb = a.bit_length() - 1, b.bit_length() - 1
-    an, bn, e = (a << (31 - la)) >> 1, (b << (31 - lb)) >> 1, la - lb
-    if an < bn:
-        an, e = an << 1, e - 1
-    r = an - bn
-    rc = Fraction(float(np.float32(1.0) / np.float32(bn))) * 2 ** 26
-    dg = []
+    za, zb = 32 - a.bit_length(), 32 - b.bit_length()
+    an, bn = ((a << za) & 0xFFFFFFFF) >> 1, ((b << zb) & 0xFFFFFFFF) >> 1
+    c = int(an < bn)
+    r = (an << c) - bn
+    e = zb - za - c
+    # bn * 2^-27 as an FP32 from the top 24 bits of bn (truncated), then its reciprocal
+    bt = np.array([0x40800000 + (bn >> 7)], dtype=np.uint32).view(np.float32)[0]
+    assert Fraction(float(bt)) == Fraction((bn >> 7) << 7, 2 ** 27)
+    rcp = np.float32(1.0) / bt
+    rcp = (np.array([rcp], dtype=np.float32).view(np.int32) + ulps).view(np.float32)[0]
+    rc = Fraction(float(rcp))
+    d = []
     for _ in range(3):
-        t = Fraction(r >> 8) * rc  # the FMA's exact product
-        assert abs(t - Fraction(r << 18, bn)) < Fraction(1, 4)
+        assert -(2 ** 22) <= r >> 9 < 2 ** 22  # exact through the 1.5 * 2^23 offset
+        t = Fraction(r >> 9) * rc  # the FMA's exact product
+        assert abs(t - Fraction(r << 18, bn)) < (Fraction(1, 4) if ulps == 0 else Fraction(1, 2))
         q = round(t)  # round half to even, as the FP32 offset addition does
-        rem = (r << 18) - q * bn
-        assert -bn <= rem < bn
-        if rem < 0:
-            q, rem = q - 1, rem + bn
-        dg.append(q)
-        r = rem
-    mant = (dg[0] << 34) | (dg[1] << 16) | (dg[2] >> 2)
-    guard = (dg[2] >> 1) & 1
-    sticky = (dg[2] & 1) or r != 0
-    if guard and (sticky or (mant & 1)):
-        mant += 1
+        r = (r << 18) - q * bn
+        assert -bn < r < bn  # fits an int32, so the device's wrapping arithmetic is exact
+        d.append(q)
+    F = (d[0] << 36) + (d[1] << 18) + d[2]
+    assert 0 <= F < 2 ** 54
+    mant = (F + 2 - int(r < 0)) >> 2
     return sign | (((e + 1023) << 52) + mant)
 
 
@@ -274,6 +275,11 @@ def test_int32_division_to_float64_is_correctly_rounded():
         else:
             exp = struct.unpack("<Q", struct.pack("<d", float(x) / float(y)))[0]
         assert _int32_div_f64_bits(x, y) == exp, (x, y)
+    # the reciprocal one ulp either way (rcp.approx's error) gives the same bits
+    for x, y in cases[:6000]:
+        if y != 0:
+            exp = _int32_div_f64_bits(x, y)
+            assert _int32_div_f64_bits(x, y, 1) == exp and _int32_div_f64_bits(x, y, -1) == exp, (x, y)
 
 
 def _header_functions():
