@@ -35,10 +35,19 @@ int32_t launch_reduce_pooled(RedArgs a, const RedShape& sh);                  //
 constexpr int64_t DEFAULT_CHUNK = 32768;  // elements per work item (16384: 3.19 ms, 32768: 3.15 ms on 10,000 tasks)
 constexpr int64_t WALK_ELEMS = 512;       // reduced elements one thread walks per unit, about at most
 
-static BatchKernel pick_kernel(bool narrow, int nin, bool wide) {
-  if (narrow && !wide) return nin <= 2 ? batch_kernel_u32_nin2() : batch_kernel_u32_nin4();
-  return batch_kernel_u64();
+static BatchKernel pick_kernel(int cls, bool narrow, int nin, bool wide) {
+  if (cls == BC_REDUCE) return batch_kernel_reduce(wide);
+  if (narrow) return nin <= 2 ? batch_kernel_u32_nin2(cls) : batch_kernel_u32_nin4(cls);
+  return batch_kernel_u64(cls);
 }
+
+// One launch per body class present: its kernel, launch shape and items.
+struct Phase {
+  BatchKernel kernel = nullptr;
+  size_t smem = 0;
+  int grid = 0;
+  int64_t begin = 0, end = 0;
+};
 
 // The per-op replay of a reduction task: the standalone plan and launch shape.
 struct Replay {
@@ -53,15 +62,13 @@ struct Batch {
   BTask* d_tasks = nullptr;
   int32_t* d_item_task = nullptr;
   phcu_program_t* d_progs = nullptr;
-  unsigned long long* d_ticket = nullptr;
+  unsigned long long* d_ticket = nullptr;  // one counter per phase
   uint32_t* d_counters = nullptr;
   Partial* d_partials = nullptr;
   int64_t n_items = 0;
   int32_t n_counters = 0;
   int64_t bytes = 0;
-  size_t smem = 0;
-  BatchKernel kernel = nullptr;
-  int grid = 0;
+  Phase phases[BC_COUNT];  // one per body class
   cudaGraphExec_t graph = nullptr;
   cudaStream_t graph_stream = nullptr;
 };
@@ -130,7 +137,7 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
     fill_prog.push_back({dtype, (int)b->host_progs.size() - 1});
     return (int)b->host_progs.size() - 1;
   };
-  bool narrow = true, wide = false;
+  bool narrow = true, wide = false;  // elementwise programs all 32-bit; any 64-bit reduction
   int nin_max = 0, max_staged = 0;
   auto fail_batch = [&](int32_t rc) {
     free_batch(b);
@@ -217,9 +224,9 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
       return fail_batch(fail(PHCU_ERR_INVALID, "batch task %d: unknown kind %d", i, t.kind));
     }
     bt.h.nitems = (bt.h.nunits + bt.h.per_item - 1) / bt.h.per_item;
-    // order: body (kind, interpreter or layout, chunk width, operator), then size, largest first
-    bt.order_key = bt.h.kind == BK_REDUCE ? 64 + bt.h.rmode * 2 + (bt.ra.op == PHCU_RED_SUM)
-                                          : (bt.h.kind * 4 + bt.h.fast) * 2 + (bt.h.vec == 4);
+    // order: body class, then layout, chunk width or operator, then size, largest first
+    bt.order_key = body_class(bt.h.kind, bt.h.fast) * 8 +
+                   (bt.h.kind == BK_REDUCE ? bt.h.rmode * 2 + (bt.ra.op == PHCU_RED_SUM) : (bt.h.vec == 4));
     b->bytes += bt.bytes;
     b->host_tasks.push_back(bt);
   }
@@ -263,7 +270,7 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
   if (e == cudaSuccess) e = cudaMalloc(&b->d_item_task, std::max<size_t>(1, item_task.size()) * sizeof(int32_t));
   if (e == cudaSuccess)
     e = cudaMalloc(&b->d_progs, std::max<size_t>(1, b->host_progs.size()) * sizeof(phcu_program_t));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_ticket, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_ticket, BC_COUNT * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_counters, std::max(1, b->n_counters) * sizeof(uint32_t));
   if (e != cudaSuccess) return fail_batch(cuda_fail(e, "cudaMalloc(batch)"));
   if (!b->host_tasks.empty())
@@ -277,21 +284,32 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
                         cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return fail_batch(cuda_fail(e, "batch upload"));
-  b->kernel = pick_kernel(narrow, nin_max, wide);
-  b->smem = (size_t)max_staged * TILE * (TILE + 1) * ((narrow && !wide) ? 4 : 8);
-  // static + dynamic shared memory above the default 48 KiB needs an opt-in
-  cudaFuncAttributes fa;
-  e = cudaFuncGetAttributes(&fa, (const void*)b->kernel);
-  if (e != cudaSuccess) return fail_batch(cuda_fail(e, "cudaFuncGetAttributes(batch_kernel)"));
-  if (fa.sharedSizeBytes + b->smem > 48 * 1024) {
-    e = cudaFuncSetAttribute((const void*)b->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem);
-    if (e != cudaSuccess) return fail_batch(cuda_fail(e, "cudaFuncSetAttribute(batch_kernel)"));
+  // the items of each body class are contiguous (the order key starts with
+  // the class); each class gets its own kernel and launch
+  for (const BTask& bt : b->host_tasks) {
+    Phase& ph = b->phases[body_class(bt.h.kind, bt.h.fast)];
+    if (ph.end == 0) ph.begin = bt.h.item0;
+    ph.end = bt.h.item0 + bt.h.nitems;
   }
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)b->kernel, BATCH_THREADS, b->smem);
-  if (e != cudaSuccess) return fail_batch(cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor(batch)"));
-  if (per_sm < 1) per_sm = 1;
-  b->grid = ctx().sm_count * per_sm;
+  for (int cls = 0; cls < BC_COUNT; cls++) {
+    Phase& ph = b->phases[cls];
+    if (ph.end <= ph.begin) continue;
+    ph.kernel = pick_kernel(cls, narrow, nin_max, wide);
+    ph.smem = (cls == BC_TILE || cls == BC_TILE_FX) ? (size_t)max_staged * TILE * (TILE + 1) * (narrow ? 4 : 8) : 0;
+    // static + dynamic shared memory above the default 48 KiB needs an opt-in
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, (const void*)ph.kernel);
+    if (e != cudaSuccess) return fail_batch(cuda_fail(e, "cudaFuncGetAttributes(batch_kernel)"));
+    if (fa.sharedSizeBytes + ph.smem > 48 * 1024) {
+      e = cudaFuncSetAttribute((const void*)ph.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ph.smem);
+      if (e != cudaSuccess) return fail_batch(cuda_fail(e, "cudaFuncSetAttribute(batch_kernel)"));
+    }
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)ph.kernel, BATCH_THREADS, ph.smem);
+    if (e != cudaSuccess) return fail_batch(cuda_fail(e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor(batch)"));
+    if (per_sm < 1) per_sm = 1;
+    ph.grid = (int)std::min<int64_t>((int64_t)ctx().sm_count * per_sm, ph.end - ph.begin);
+  }
   *out = b;
   return PHCU_OK;
 }
@@ -301,21 +319,26 @@ int32_t batch_launch(Batch* b, int mode) {
   cudaStream_t s = stream();
   if (b->n_items == 0) return PHCU_OK;
   if (mode == 0) {
-    PHCU_CUDA(cudaMemsetAsync(b->d_ticket, 0, sizeof(unsigned long long), s));
+    PHCU_CUDA(cudaMemsetAsync(b->d_ticket, 0, BC_COUNT * sizeof(unsigned long long), s));
     if (b->n_counters) PHCU_CUDA(cudaMemsetAsync(b->d_counters, 0, b->n_counters * sizeof(uint32_t), s));
-    BatchArgs A;
-    A.tasks = b->d_tasks;
-    A.item_task = b->d_item_task;
-    A.progs = b->d_progs;
-    A.ticket = b->d_ticket;
-    A.counters = b->d_counters;
-    A.status = ctx().status;
-    A.n_items = b->n_items;
-    A.deadline_ns = 20ull * 1000 * 1000 * 1000;  // 20 s
-    int grid = (int)std::min<int64_t>(b->grid, b->n_items);
-    b->kernel<<<grid, BATCH_THREADS, b->smem, s>>>(A);
-    count_launch();
-    return check_launch("batch_kernel");
+    for (int cls = 0; cls < BC_COUNT; cls++) {
+      const Phase& ph = b->phases[cls];
+      if (!ph.kernel) continue;
+      BatchArgs A;
+      A.tasks = b->d_tasks;
+      A.item_task = b->d_item_task;
+      A.progs = b->d_progs;
+      A.ticket = b->d_ticket + cls;
+      A.counters = b->d_counters;
+      A.status = ctx().status;
+      A.item_begin = ph.begin;
+      A.item_end = ph.end;
+      A.deadline_ns = 20ull * 1000 * 1000 * 1000;  // 20 s
+      ph.kernel<<<ph.grid, BATCH_THREADS, ph.smem, s>>>(A);
+      count_launch();
+      PHCU_TRY(check_launch("batch_kernel"));
+    }
+    return PHCU_OK;
   }
   if (mode == 2 && b->graph && b->graph_stream == s) {
     PHCU_CUDA(cudaGraphLaunch(b->graph, s));

@@ -16,6 +16,13 @@ namespace phcu {
 
 enum BKind : int32_t { BK_ROW = 0, BK_TILE = 1, BK_REDUCE = 2 };
 
+// Body classes, in item order (one launch each): the layout and, for the
+// elementwise layouts, the interpreter (general or pre-decoded).
+enum BClass : int32_t { BC_ROW = 0, BC_ROW_FX = 1, BC_TILE = 2, BC_TILE_FX = 3, BC_REDUCE = 4, BC_COUNT = 5 };
+__host__ __device__ inline int body_class(int kind, int fast) {
+  return kind == BK_REDUCE ? BC_REDUCE : kind * 2 + (fast == FAST_FX);
+}
+
 // What a block needs to run one task's items (staged in shared memory).
 struct BHead {
   int32_t kind;
@@ -42,6 +49,9 @@ constexpr int BATCH_THREADS = 256;
 #define PHCU_BATCH_MIN_BLOCKS 3
 #endif
 constexpr int BATCH_MIN_BLOCKS = PHCU_BATCH_MIN_BLOCKS;
+#ifndef PHCU_BATCH_ROW_FX_BLOCKS
+#define PHCU_BATCH_ROW_FX_BLOCKS 3
+#endif
 // The bodies are inlined into the kernel.  As separate functions (built with
 // PHCU_BATCH_NOINLINE) each keeps its own register allocation but the calls
 // spill: the 10,000-task workload took 3.59 ms so, 3.35 ms inlined, and
@@ -76,15 +86,6 @@ constexpr int batch_v() {
   return (sizeof(S) == 8 || FAST == FAST_NONE) ? 4 : 8;
 }
 
-template <typename S, int NIN, int FAST>
-__device__ __forceinline__ void row_fast(const BHead& h, const EvalPlan& p, const phcu_program_t& prog, int64_t u0,
-                                         int64_t u1, uint32_t& st) {
-  constexpr int V = batch_v<S, FAST>();
-  constexpr bool STASH = FAST == FAST_NONE;
-  if (h.vec == 4) row_item<S, NIN, 4, V / 4, STASH, FAST>(p, prog, u0, u1, st);
-  else row_item<S, NIN, 1, V / 2, STASH, FAST>(p, prog, u0, u1, st);
-}
-
 // One function per body and chunk width: each gets its own register allocation.
 template <typename S, int NIN, int VEC, int FAST>
 __device__ PHCU_BODY void run_row_body(const EvalPlan& p, const phcu_program_t& prog, int64_t u0, int64_t u1,
@@ -93,30 +94,11 @@ __device__ PHCU_BODY void run_row_body(const EvalPlan& p, const phcu_program_t& 
   row_item<S, NIN, VEC, VEC == 4 ? V / 4 : V / 2, FAST == FAST_NONE, FAST>(p, prog, u0, u1, st);
 }
 
-template <typename S, int NIN>
-__device__ __forceinline__ void run_row(const BHead& h, const EvalPlan& p, const phcu_program_t& prog, int64_t u0,
-                                        int64_t u1, uint32_t& st) {
-  if (h.fast == FAST_FX) {
-    if (h.vec == 4) run_row_body<S, NIN, 4, FAST_FX>(p, prog, u0, u1, st);
-    else run_row_body<S, NIN, 1, FAST_FX>(p, prog, u0, u1, st);
-  } else {
-    if (h.vec == 4) run_row_body<S, NIN, 4, FAST_NONE>(p, prog, u0, u1, st);
-    else run_row_body<S, NIN, 1, FAST_NONE>(p, prog, u0, u1, st);
-  }
-}
-
 // ----------------------------------------------------------- TILE bodies
 template <typename S, int NIN, int FAST>
 __device__ PHCU_BODY void run_tile_body(const EvalPlan& p, const phcu_program_t& prog, int64_t u0, int64_t u1,
                                            S* tiles, uint32_t& st) {
   for (int64_t t = u0; t < u1; t++) tile_body<S, NIN, FAST == FAST_NONE, FAST>(p, prog, (uint64_t)t, tiles, st);
-}
-
-template <typename S, int NIN>
-__device__ __forceinline__ void run_tile(const BHead& h, const EvalPlan& p, const phcu_program_t& prog, int64_t u0,
-                                         int64_t u1, S* tiles, uint32_t& st) {
-  if (h.fast == FAST_FX) run_tile_body<S, NIN, FAST_FX>(p, prog, u0, u1, tiles, st);
-  else run_tile_body<S, NIN, FAST_NONE>(p, prog, u0, u1, tiles, st);
 }
 
 // ------------------------------------------------------ REDUCE bodies
@@ -202,55 +184,62 @@ struct BatchArgs {
   const BTask* tasks;
   const int32_t* item_task;
   const phcu_program_t* progs;
-  unsigned long long* ticket;
+  unsigned long long* ticket;  // this launch's own counter, from 0
   uint32_t* counters;
   uint32_t* status;
-  int64_t n_items;
-  uint64_t deadline_ns;  // global-timer budget per launch
+  int64_t item_begin, item_end;  // the items of this launch's body class
+  uint64_t deadline_ns;          // global-timer budget per launch
 };
 
-constexpr size_t PLAN_BYTES = sizeof(EvalPlan) > sizeof(RedArgs) ? sizeof(EvalPlan) : sizeof(RedArgs);
+// Resident blocks per SM of each class's kernel.
+template <int CLASS>
+constexpr int batch_min_blocks() {
+  return CLASS == BC_ROW_FX ? PHCU_BATCH_ROW_FX_BLOCKS : BATCH_MIN_BLOCKS;
+}
 
+// One persistent kernel per body class (BClass), each compiled with only that
+// class's bodies, so each gets the register allocation its own bodies need.
 // S: program slot width; NIN: inputs per program (2 or 4); WIDE: reductions
-// of 64-bit elements.  Blocks take items with an atomic ticket until the list
-// (or the global-timer deadline) runs out; a task's plan and program are
-// copied into shared memory when the block's task changes.
-template <typename S, int NIN, bool WIDE>
-__global__ void __launch_bounds__(BATCH_THREADS, BATCH_MIN_BLOCKS) batch_kernel(const __grid_constant__ BatchArgs A) {
+// of 64-bit elements.  Blocks take the class's items with an atomic ticket
+// until they (or the global-timer deadline) run out; a task's plan (and
+// program) is copied into shared memory when the block's task changes.
+template <typename S, int NIN, bool WIDE, int CLASS>
+__global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks<CLASS>())
+    batch_kernel(const __grid_constant__ BatchArgs A) {
   extern __shared__ __align__(16) unsigned char tiles_raw[];
   S* tiles = reinterpret_cast<S*>(tiles_raw);
-  __shared__ __align__(16) unsigned char s_plan[PLAN_BYTES];
-  __shared__ __align__(16) phcu_program_t s_prog;
+  constexpr size_t PB = CLASS == BC_REDUCE ? sizeof(RedArgs) : sizeof(EvalPlan);
+  __shared__ __align__(16) unsigned char s_plan[PB];
+  // the program (elementwise classes) or the fold scratch (reductions)
+  __shared__ __align__(16) unsigned char s_aux[CLASS == BC_REDUCE ? sizeof(CombineScratch) : sizeof(phcu_program_t)];
   __shared__ BHead s_head;
   __shared__ long long s_item;
   __shared__ int s_flag;
-  __shared__ CombineScratch s_combine;
+  const phcu_program_t& s_prog = *reinterpret_cast<const phcu_program_t*>(s_aux);
   uint32_t st = 0;
   int cur = -1;  // task whose plan is in shared memory
   const uint64_t t_start = global_ns();
   for (;;) {
     if (threadIdx.x == 0) {
-      long long it = (long long)atomicAdd(A.ticket, 1ull);
+      long long it = A.item_begin + (long long)atomicAdd(A.ticket, 1ull);
       if (global_ns() - t_start > A.deadline_ns) {
         st |= PHCU_ST_TIMEOUT;
-        it = A.n_items;  // give up: the host sees TIMEOUT in the status word
+        it = A.item_end;  // give up: the host sees TIMEOUT in the status word
       }
       s_item = it;
     }
     __syncthreads();
     const long long item = s_item;
-    if (item >= A.n_items) break;
+    if (item >= A.item_end) break;
     const int ti = A.item_task[item];
     if (ti != cur) {  // uniform: every thread read the same item
       const BTask& T = A.tasks[ti];
-      const bool red = T.h.kind == BK_REDUCE;
-      const uint32_t* src = red ? (const uint32_t*)&T.ra : (const uint32_t*)&T.ep;
-      const int words = (int)((red ? sizeof(RedArgs) : sizeof(EvalPlan)) / 4);
-      for (int i = threadIdx.x; i < words; i += blockDim.x) ((uint32_t*)s_plan)[i] = src[i];
-      if (!red) {
+      const uint32_t* src = CLASS == BC_REDUCE ? (const uint32_t*)&T.ra : (const uint32_t*)&T.ep;
+      for (int i = threadIdx.x; i < (int)(PB / 4); i += blockDim.x) ((uint32_t*)s_plan)[i] = src[i];
+      if constexpr (CLASS != BC_REDUCE) {
         const uint32_t* ps = (const uint32_t*)&A.progs[T.prog];
         for (int i = threadIdx.x; i < (int)(sizeof(phcu_program_t) / 4); i += blockDim.x)
-          ((uint32_t*)&s_prog)[i] = ps[i];
+          ((uint32_t*)s_aux)[i] = ps[i];
       }
       if (threadIdx.x == 0) s_head = T.h;
       cur = ti;
@@ -260,10 +249,14 @@ __global__ void __launch_bounds__(BATCH_THREADS, BATCH_MIN_BLOCKS) batch_kernel(
     const int64_t local = item - h.item0;
     const int64_t u0 = local * h.per_item;
     const int64_t u1 = min(h.nunits, u0 + h.per_item);
-    if (h.kind == BK_ROW) {
-      run_row<S, NIN>(h, *reinterpret_cast<const EvalPlan*>(s_plan), s_prog, u0, u1, st);
-    } else if (h.kind == BK_TILE) {
-      run_tile<S, NIN>(h, *reinterpret_cast<const EvalPlan*>(s_plan), s_prog, u0, u1, tiles, st);
+    if constexpr (CLASS == BC_ROW || CLASS == BC_ROW_FX) {
+      constexpr int FAST = CLASS == BC_ROW_FX ? FAST_FX : FAST_NONE;
+      const EvalPlan& p = *reinterpret_cast<const EvalPlan*>(s_plan);
+      if (h.vec == 4) run_row_body<S, NIN, 4, FAST>(p, s_prog, u0, u1, st);
+      else run_row_body<S, NIN, 1, FAST>(p, s_prog, u0, u1, st);
+    } else if constexpr (CLASS == BC_TILE || CLASS == BC_TILE_FX) {
+      constexpr int FAST = CLASS == BC_TILE_FX ? FAST_FX : FAST_NONE;
+      run_tile_body<S, NIN, FAST>(*reinterpret_cast<const EvalPlan*>(s_plan), s_prog, u0, u1, tiles, st);
     } else {
       const RedArgs& a = *reinterpret_cast<const RedArgs*>(s_plan);
       run_reduce<WIDE>(h, a, u0, u1, st);
@@ -277,7 +270,7 @@ __global__ void __launch_bounds__(BATCH_THREADS, BATCH_MIN_BLOCKS) batch_kernel(
         __syncthreads();
         if (s_flag) {
           __threadfence();
-          run_combine<WIDE>(a, s_combine, st);
+          run_combine<WIDE>(a, *reinterpret_cast<CombineScratch*>(s_aux), st);
         }
       }
     }
@@ -288,9 +281,21 @@ __global__ void __launch_bounds__(BATCH_THREADS, BATCH_MIN_BLOCKS) batch_kernel(
 
 using BatchKernel = void (*)(BatchArgs);
 
-// The instantiations (batch_k32n2.cu, batch_k32n4.cu, batch_k64.cu).
-BatchKernel batch_kernel_u32_nin2();
-BatchKernel batch_kernel_u32_nin4();
-BatchKernel batch_kernel_u64();
+// The instantiations (batch_k32n2.cu, batch_k32n4.cu, batch_k64.cu): the
+// elementwise classes per slot width and input count, the reductions narrow
+// (32-bit elements) and wide (every element type).
+template <typename S, int NIN>
+inline BatchKernel batch_kernel_ew(int cls) {
+  switch (cls) {
+    case BC_ROW: return batch_kernel<S, NIN, false, BC_ROW>;
+    case BC_ROW_FX: return batch_kernel<S, NIN, false, BC_ROW_FX>;
+    case BC_TILE: return batch_kernel<S, NIN, false, BC_TILE>;
+    default: return batch_kernel<S, NIN, false, BC_TILE_FX>;
+  }
+}
+BatchKernel batch_kernel_u32_nin2(int cls);
+BatchKernel batch_kernel_u32_nin4(int cls);
+BatchKernel batch_kernel_u64(int cls);
+BatchKernel batch_kernel_reduce(bool wide);
 
 }  // namespace phcu

@@ -270,6 +270,11 @@ __device__ __forceinline__ void finish(const RedArgs& a, int64_t o, int64_t spli
   if (KIND == RK_SUM) {
     if constexpr (std::is_same<T, int32_t>::value || std::is_same<T, long long>::value) {
       store_final(a, o, 0, 0, true, (long long)sacc.s, 0, st);
+    } else if constexpr (std::is_same<T, float>::value) {
+      // s + c rounded once to FP32 (the correctly rounded value of the pair);
+      // FP64 conversions cost as much as many loads on this part
+      if (a.out_dtype == PHCU_F32 && !a.want_index) *(float*)(a.out + o * 4) = sacc.s + sacc.c;
+      else store_final(a, o, sacc.value(), 0, false, 0, 0, st);
     } else {
       store_final(a, o, sacc.value(), 0, false, 0, 0, st);
     }
@@ -282,10 +287,16 @@ __device__ __forceinline__ void finish(const RedArgs& a, int64_t o, int64_t spli
       idx = 0;
       v = first;
     }
-    double d;
-    long long l;
-    ext_parts<T>(v, d, l);
-    store_final(a, o, d, l, false, 0, idx, st);
+    if (a.want_index) {
+      store_final(a, o, 0, 0, false, 0, idx, st);
+    } else if (std::is_same<T, float>::value && a.out_dtype == PHCU_F32) {
+      *(T*)(a.out + o * sizeof(T)) = v;  // the element itself, no conversion
+    } else {
+      double d;
+      long long l;
+      ext_parts<T>(v, d, l);
+      store_final(a, o, d, l, false, 0, idx, st);
+    }
   }
 }
 
@@ -539,16 +550,12 @@ __device__ __forceinline__ void group_vec(const RedArgs& a, int64_t o0, int64_t 
 
 // COLUMN with 16-byte loads across outputs: one thread reduces VN consecutive
 // outputs o0 .. o0 + VN - 1, which are consecutive in memory (the innermost
-// kept axis has unit stride and a length divisible by VN).  Reduced positions
-// in flight: eight for extrema (four: 2-7% slower on 64x128x128x64, axes
-// 0-2), four for compensated floating-point sums, whose adds then interleave
-// with the next loads (a [64, 128, 8192] column sum: 49.3 -> 43.6 us; sixteen:
-// 51.4 us).  Requires every output row start and every reduced stride to be
-// 16-byte aligned.
-template <typename T, int KIND>
-constexpr int col_inflight() {
-  return (KIND == RK_SUM && (std::is_same<T, float>::value || std::is_same<T, double>::value)) ? 4 : 8;
-}
+// kept axis has unit stride and a length divisible by VN), eight reduced
+// positions in flight (four: 2-7% slower for extrema and 4-7% for sums on
+// 64x128x128x64, axes 0-2; sixteen: slower for sums).  Requires every output
+// row start and every reduced stride to be 16-byte aligned.
+constexpr int COL_INFLIGHT = 8;
+
 template <typename T, int KIND>
 __device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t split, uint32_t& st) {
   constexpr int VN = 16 / sizeof(T);
@@ -567,7 +574,7 @@ __device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t
   if (a.krank == 1) {
     const int64_t ks = a.kinner * (int64_t)sizeof(T);
     const char* p = base + k0 * ks;
-    constexpr int NF = col_inflight<T, KIND>();
+    constexpr int NF = COL_INFLIGHT;
     for (; k + NF - 1 < k1; k += NF, p += NF * ks) {
       T x[NF][VN];
 #pragma unroll
@@ -602,6 +609,76 @@ __device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t
   }
 #pragma unroll
   for (int e = 0; e < VN; e++) finish<T, KIND>(a, o0 + e, split, sacc[e], eacc[e], st);
+}
+
+// SLAB: the reduced axis sits directly outside the innermost kept axis and
+// the two form one contiguous slab of K rows of L elements (L * K elements
+// per slab, one slab per value of the outer kept axes).  The block reads a
+// slab front to back: thread t takes vector t % LV of each row (LV = L / VN)
+// and rows t / LV, t / LV + RPI, ... (RPI = 256 / LV), eight in flight, so a
+// warp's loads cover whole rows and the block's 4 KB in a row.  Row partials
+// meet in shared memory, where thread l < L folds those of output l in row
+// order and finishes it.  Needs a.S == 1 and LV a power of two <= 256.
+constexpr int SLAB_THREADS = 256;
+template <typename T, int KIND>
+using SlabAcc = typename std::conditional<KIND == RK_SUM, SumAcc<T>, ExtAcc<T>>::type;
+
+template <typename T, int KIND>
+__device__ __forceinline__ void column_slab(const RedArgs& a, int64_t slab, int L, SlabAcc<T, KIND>* sh, uint32_t& st) {
+  constexpr int VN = 16 / sizeof(T);
+  const bool is_max = (a.op == PHCU_RED_MAX || a.op == PHCU_RED_ARGMAX);
+  const int LV = L / VN, RPI = SLAB_THREADS / LV;
+  const int lv = threadIdx.x % LV, rr = threadIdx.x / LV;
+  const int64_t o0 = slab * L;
+  const char* base = a.in + (out_offset(a, (uint32_t)o0) + (int64_t)lv * VN) * (int64_t)sizeof(T);
+  const int64_t rs = (int64_t)L * sizeof(T);  // bytes per row
+  SlabAcc<T, KIND> acc[VN];
+#pragma unroll
+  for (int e = 0; e < VN; e++) acc[e].init();
+  int64_t k = rr;
+  for (; k + (int64_t)(COL_INFLIGHT - 1) * RPI < a.K; k += (int64_t)COL_INFLIGHT * RPI) {
+    T x[COL_INFLIGHT][VN];
+#pragma unroll
+    for (int j = 0; j < COL_INFLIGHT; j++) ld16<T>(base + (k + (int64_t)j * RPI) * rs, x[j]);
+#pragma unroll
+    for (int j = 0; j < COL_INFLIGHT; j++)
+#pragma unroll
+      for (int e = 0; e < VN; e++) {
+        if constexpr (KIND == RK_SUM) acc[e].add(x[j][e]);
+        else acc[e].add(x[j][e], k + (int64_t)j * RPI, is_max);
+      }
+  }
+  for (; k < a.K; k += RPI) {
+    T x[VN];
+    ld16<T>(base + k * rs, x);
+#pragma unroll
+    for (int e = 0; e < VN; e++) {
+      if constexpr (KIND == RK_SUM) acc[e].add(x[e]);
+      else acc[e].add(x[e], k, is_max);
+    }
+  }
+  // partial of row set rr for output lv * VN + e at sh[rr * L + lv * VN + e]
+#pragma unroll
+  for (int e = 0; e < VN; e++) sh[rr * L + lv * VN + e] = acc[e];
+  __syncthreads();
+  for (int l = threadIdx.x; l < L; l += SLAB_THREADS) {
+    SlabAcc<T, KIND> r = sh[l];
+    for (int j = 1; j < RPI; j++) {
+      if constexpr (KIND == RK_SUM) r.merge(sh[j * L + l]);
+      else r.merge(sh[j * L + l], is_max);
+    }
+    SumAcc<T> sacc;
+    ExtAcc<T> eacc;
+    if constexpr (KIND == RK_SUM) {
+      sacc = r;
+      eacc.init();
+    } else {
+      eacc = r;
+      sacc.init();
+    }
+    finish<T, KIND>(a, o0 + l, 0, sacc, eacc, st);
+  }
+  __syncthreads();
 }
 
 // COLUMN: one thread reduces elements [k0, k1) of output o.
@@ -682,10 +759,16 @@ __device__ __forceinline__ void combine_one(const RedArgs& a, int64_t o, uint32_
       idx = 0;
       v = first;
     }
-    double d;
-    long long l;
-    ext_parts<T>(v, d, l);
-    store_final(a, o, d, l, false, 0, idx, st);
+    if (a.want_index) {
+      store_final(a, o, 0, 0, false, 0, idx, st);
+    } else if (std::is_same<T, float>::value && a.out_dtype == PHCU_F32) {
+      *(T*)(a.out + o * sizeof(T)) = v;  // the element itself, no conversion
+    } else {
+      double d;
+      long long l;
+      ext_parts<T>(v, d, l);
+      store_final(a, o, d, l, false, 0, idx, st);
+    }
   }
 }
 

@@ -382,3 +382,34 @@ def test_empty_and_degenerate(cu, ora):
     C = A.clone()
     C[cu.R(0, 1), slice(None)] = C.view(cu.R(1, 2), slice(None))
     assert C.to_narr()[:2].tolist() == a[1:3].tolist()
+
+
+@pytest.mark.parametrize("view", ["plain", "reverse", "permute"])
+def test_int32_division_kernel(cu, view):
+    """Int32 / Int32 -> Float64 through its own kernel kind (ROW for plain and
+    reversed views, TMA tiles for permuted ones), bit-exact against IEEE
+    division on the host, with zero divisors and dividends, Int32::MIN and
+    exact quotients among random pairs."""
+    rng = np.random.default_rng(7)
+    shape = [96, 130, 72]
+    a = rng.integers(-2 ** 31, 2 ** 31, shape, dtype=np.int64).astype(np.int32)
+    b = rng.integers(-2 ** 31, 2 ** 31, shape, dtype=np.int64).astype(np.int32)
+    fa, fb = a.reshape(-1), b.reshape(-1)
+    fb[::7] = rng.integers(-1000, 1000, fb[::7].size)
+    fb[3::101] = 0
+    fa[5::103] = 0
+    fa[11::211] = -2 ** 31
+    fb[17::223] = -2 ** 31
+    fa[19::97] = fb[19::97] * 3  # exact quotients (wrapping is fine: still Int32 pairs)
+    A_, B_ = cu.CuNArray.from_numpy(a), cu.CuNArray.from_numpy(b)
+    if view == "reverse":
+        A_, B_, a, b = A_.reverse(), B_.reverse(), a[::-1, ::-1, ::-1], b[::-1, ::-1, ::-1]
+    elif view == "permute":
+        A_, B_, a, b = A_.permute(2, 0, 1), B_.permute(2, 0, 1), a.transpose(2, 0, 1), b.transpose(2, 0, 1)
+    got = (A_ / B_).to_narr()
+    with np.errstate(divide="ignore", invalid="ignore"):
+        exp = a.astype(np.float64) / b.astype(np.float64)
+    assert got.dtype == np.float64
+    nan = np.isnan(exp)
+    assert np.array_equal(np.isnan(got), nan)
+    assert np.array_equal(got[~nan].view(np.uint64), exp[~nan].view(np.uint64))

@@ -116,3 +116,33 @@ def test_column_layouts(cu, ora, dt, shape, axis):
         fin = np.isfinite(ref)
         assert np.all(np.abs(s[fin] - ref[fin]) <= 1e-6 * mag[fin] + 1e-30)  # 1e-6 of the sum of magnitudes
         assert np.all(np.isnan(s[~fin]))
+
+
+# SLAB sums: the reduced axis directly outside the innermost kept axis, the
+# two contiguous (one K x L slab per outer index), L / (16 / element size) a
+# power of two up to 256, one split (at least 1024 outputs per SM) and enough
+# slabs for every SM.  Odd K leaves tails after the eight-in-flight batches;
+# L = 8 gives 128 row sets per block, L = 1024 a single one (Float64: COLUMN).
+@pytest.mark.parametrize("dt", [np.float32, np.int32, np.float64])
+@pytest.mark.parametrize("shape", [[2500, 37, 64], [20000, 33, 8], [160, 20, 1024], [3, 820, 9, 64]])
+def test_slab_sums(cu, ora, dt, shape):
+    axis = len(shape) - 2
+    rng = np.random.default_rng(sum(shape))
+    if np.issubdtype(dt, np.integer):
+        x = rng.integers(-1000, 1000, shape).astype(dt)
+    else:
+        x = (rng.standard_normal(shape) * 10).astype(dt)
+        flat = x.reshape(-1)
+        flat[13::1009] = np.nan
+        flat[::4099] = 1e30  # large terms next to small ones: the compensation matters
+    X = cu.CuNArray.from_numpy(x)
+    s = X.sum(axis=axis).to_narr()
+    if dt == np.int32:
+        assert np.array_equal(s, ora.reduce(ora.RED_SUM, x, axis))
+    else:
+        ref, mag = ora.reduce_f64(x, axis), ora.reduce_f64(np.abs(x), axis)
+        fin = np.isfinite(ref)
+        assert np.all(np.abs(s[fin] - ref[fin]) <= 1e-6 * mag[fin] + 1e-30)  # 1e-6 of the sum of magnitudes
+        assert np.all(np.isnan(s[~fin]))
+    # the extrema of the same layouts stay in COLUMN and stay exact
+    assert np.array_equal(X.argmax(axis=axis).to_narr(), ora.reduce(ora.RED_ARGMAX, x, axis, ora.I32))
