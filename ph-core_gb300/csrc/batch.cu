@@ -217,7 +217,9 @@ int32_t batch_prepare(const phcu_task_t* tasks, int32_t n, const phcu_program_t*
         if (dtype_size(bt.ra.dtype) == 8) wide = true;
         batch_splits(bt.ra, rmode, bt.h.rG);
         bt.h.nunits = bt.ra.O * bt.ra.S;
-        bt.h.per_item = std::max<int64_t>(1, chunk / std::max<int64_t>(1, bt.ra.chunk));
+        // at least one unit for every group of lanes of the block: a smaller
+        // item leaves threads idle at the item's closing barrier
+        bt.h.per_item = std::max<int64_t>(chunk / std::max<int64_t>(1, bt.ra.chunk), BATCH_THREADS / bt.h.rG);
         bt.bytes = view_size(&t.in[0]) * dtype_size(t.in[0].dtype) + bt.ra.O * dtype_size(t.out.dtype);
       }
     } else {

@@ -50,7 +50,7 @@ constexpr int BATCH_THREADS = 256;
 #endif
 constexpr int BATCH_MIN_BLOCKS = PHCU_BATCH_MIN_BLOCKS;
 #ifndef PHCU_BATCH_ROW_FX_BLOCKS
-#define PHCU_BATCH_ROW_FX_BLOCKS 3
+#define PHCU_BATCH_ROW_FX_BLOCKS 4
 #endif
 // The bodies are inlined into the kernel.  As separate functions (built with
 // PHCU_BATCH_NOINLINE) each keeps its own register allocation but the calls
@@ -78,12 +78,16 @@ __device__ __forceinline__ void row_item(const EvalPlan& p, const phcu_program_t
     row_group<S, NIN, VEC, U, STASH, FAST>(p, prog, (uint32_t)c, step, (uint32_t)u1, st);
 }
 
-// Elements per thread per pass (as the standalone ROW kernels): pre-decoded
-// programs 8 with 32-bit slots (4 with 64-bit slots), the general
-// interpreter 4; single-element chunks take half as many.
+// Elements per thread per pass: 4 (8 for pre-decoded 32-bit programs, as in
+// the standalone ROW kernel, spilled in the batch kernel at 80 registers:
+// 2.02 ms against 2.00 ms with 4 at four blocks per SM); single-element
+// chunks take half as many.
+#ifndef PHCU_BATCH_FX_V
+#define PHCU_BATCH_FX_V 4
+#endif
 template <typename S, int FAST>
 constexpr int batch_v() {
-  return (sizeof(S) == 8 || FAST == FAST_NONE) ? 4 : 8;
+  return (sizeof(S) == 8 || FAST == FAST_NONE) ? 4 : PHCU_BATCH_FX_V;
 }
 
 // One function per body and chunk width: each gets its own register allocation.
@@ -191,10 +195,12 @@ struct BatchArgs {
   uint64_t deadline_ns;          // global-timer budget per launch
 };
 
-// Resident blocks per SM of each class's kernel.
-template <int CLASS>
+// Resident blocks per SM of each class's kernel: four for the pre-decoded
+// ROW body with 32-bit slots (64 registers; 10,000-task batch 2.15 -> 2.00
+// ms), three (80 registers) for the rest.
+template <typename S, int CLASS>
 constexpr int batch_min_blocks() {
-  return CLASS == BC_ROW_FX ? PHCU_BATCH_ROW_FX_BLOCKS : BATCH_MIN_BLOCKS;
+  return (CLASS == BC_ROW_FX && sizeof(S) == 4) ? PHCU_BATCH_ROW_FX_BLOCKS : BATCH_MIN_BLOCKS;
 }
 
 // One persistent kernel per body class (BClass), each compiled with only that
@@ -204,7 +210,7 @@ constexpr int batch_min_blocks() {
 // until they (or the global-timer deadline) run out; a task's plan (and
 // program) is copied into shared memory when the block's task changes.
 template <typename S, int NIN, bool WIDE, int CLASS>
-__global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks<CLASS>())
+__global__ void __launch_bounds__(BATCH_THREADS, batch_min_blocks<S, CLASS>())
     batch_kernel(const __grid_constant__ BatchArgs A) {
   extern __shared__ __align__(16) unsigned char tiles_raw[];
   S* tiles = reinterpret_cast<S*>(tiles_raw);

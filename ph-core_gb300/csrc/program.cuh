@@ -795,13 +795,21 @@ __device__ __forceinline__ void run_fx(int fx, int src, S imm, S* acc, const S (
 // `Float ** Int` with an immediate exponent (host check: program_is_fx).
 // Kernels built for such programs compile only these two paths: no operand
 // copies, conversions or type dispatch, so they need fewer registers.
+// A power by an immediate integer exponent (uniform across the grid): the
+// reduced interpreter runs it as binary exponentiation of its own, for Float
+// (LLVM powi) and for Int32 / Int64 (checked, or wrapping for &**).
+inline bool fx_power(const phcu_instr_t& I) {
+  if (I.src != PHCU_SRC_IMM || (I.flags & 1) || !is_int_t(I.btype)) return false;
+  if (I.op == PHCU_OP_POW) return is_float_t(I.type) || is_int_t(I.type);
+  return I.op == PHCU_OP_WPOW && is_int_t(I.type);
+}
+
 inline bool program_is_fx(const phcu_program_t& P) {
   if (P.n_instr < 1) return false;
   for (int i = 0; i < P.n_instr; i++) {
     const phcu_instr_t& I = P.code[i];
     if (I.pad[0] != FX_NONE) continue;
-    if (I.op == PHCU_OP_POW && I.src == PHCU_SRC_IMM && is_float_t(I.type) && is_int_t(I.btype) && !(I.flags & 1))
-      continue;
+    if (fx_power(I)) continue;
     return false;
   }
   return true;
@@ -819,8 +827,23 @@ __device__ __forceinline__ void run_program_fx(const phcu_program_t& P, const S 
     if (fx != FX_NONE) {
       run_fx<S, NIN, V>(fx, P.code[pc].src, (S)(uint64_t)P.code[pc].imm.i, acc, in, st);
     } else {
-      const int64_t e = P.code[pc].imm.i;
-      powi_uniform<S, V>(acc, P.code[pc].type, P.code[pc].btype == PHCU_I32 ? (int32_t)(uint32_t)e : (int32_t)e);
+      // the exponent as the general interpreter reads the immediate slot
+      const phcu_instr_t& I = P.code[pc];
+      const bool wrap = I.op == PHCU_OP_WPOW;
+      if (I.type == PHCU_I32) {
+        const int64_t e = (int32_t)(uint32_t)I.imm.i;
+#pragma unroll
+        for (int v = 0; v < V; v++) acc[v] = pi32<S>(int_pow<int32_t>(si32(acc[v]), e, wrap, st));
+      } else if (I.type == PHCU_I64) {
+        if constexpr (sizeof(S) == 8) {
+          const int64_t e = (int64_t)I.imm.i;
+#pragma unroll
+          for (int v = 0; v < V; v++) acc[v] = (S)int_pow<int64_t>((int64_t)acc[v], e, wrap, st);
+        }
+      } else {
+        const int64_t e = I.imm.i;
+        powi_uniform<S, V>(acc, I.type, I.btype == PHCU_I32 ? (int32_t)(uint32_t)e : (int32_t)e);
+      }
     }
   }
 }

@@ -413,3 +413,22 @@ def test_int32_division_kernel(cu, view):
     nan = np.isnan(exp)
     assert np.array_equal(np.isnan(got), nan)
     assert np.array_equal(got[~nan].view(np.uint64), exp[~nan].view(np.uint64))
+
+
+def test_integer_power_by_scalar(cu, ora):
+    """Int32 ** n and Int32 &** n with a scalar exponent run in the reduced
+    interpreter (binary exponentiation, checked or wrapping) and match the
+    oracle; a checked overflow raises, a negative exponent is refused."""
+    x = np.array([2, -3, 1000, 0, 1, -1, 46340, 7], dtype=np.int32)
+    X = cu.CuNArray.from_numpy(x)
+    for e in (0, 1, 2, 3):
+        exp, err = ora.map_binary_scalar(ora.OP_POW, x if e < 3 else x[:4], e, ora.I32)
+        got = ((X if e < 3 else cu.CuNArray.from_numpy(x[:4])) ** e).to_narr()
+        assert np.array_equal(got, exp), e
+    w = X.wpow(5).to_narr()
+    assert np.array_equal(w, ora.map_binary_scalar(ora.OP_WPOW, x, 5, ora.I32)[0])
+    with pytest.raises(OverflowError):
+        cu.CuNArray.from_numpy(np.array([46341, 2], np.int32)) ** 2
+    with pytest.raises(ValueError):
+        X ** -2
+    cu.check_errors()
