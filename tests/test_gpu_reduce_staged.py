@@ -122,7 +122,8 @@ def test_column_layouts(cu, ora, dt, shape, axis):
 # two contiguous (one K x L slab per outer index), L / (16 / element size) a
 # power of two up to 256, one split (at least 1024 outputs per SM) and enough
 # slabs for every SM.  Odd K leaves tails after the eight-in-flight batches;
-# L = 8 gives 128 row sets per block, L = 1024 a single one (Float64: COLUMN).
+# L = 8 gives 128 row sets per block, L = 1024 a single one (Float64: COLUMN;
+# extrema of Float64 always COLUMN).
 @pytest.mark.parametrize("dt", [np.float32, np.int32, np.float64])
 @pytest.mark.parametrize("shape", [[2500, 37, 64], [20000, 33, 8], [160, 20, 1024], [3, 820, 9, 64]])
 def test_slab_sums(cu, ora, dt, shape):
@@ -144,5 +145,19 @@ def test_slab_sums(cu, ora, dt, shape):
         fin = np.isfinite(ref)
         assert np.all(np.abs(s[fin] - ref[fin]) <= 1e-6 * mag[fin] + 1e-30)  # 1e-6 of the sum of magnitudes
         assert np.all(np.isnan(s[~fin]))
-    # the extrema of the same layouts stay in COLUMN and stay exact
-    assert np.array_equal(X.argmax(axis=axis).to_narr(), ora.reduce(ora.RED_ARGMAX, x, axis, ora.I32))
+    # extrema of the same layouts (slabs for 4-byte elements): first index of
+    # the extreme, NaNs skipped unless first, both zeros equal
+    if dt == np.float32:
+        xs = np.moveaxis(x, axis, 0)  # [K, ...]: row k of every output
+        xs[3][..., ::5] = 77.0
+        xs[6][..., ::5] = 77.0   # ties of the maximum: index 3 wins
+        xs[0][..., 1::7] = np.nan  # NaN first element: index 0 wins
+        xs[1][..., 2::11] = -0.0
+        xs[2][..., 2::11] = 0.0
+        X = cu.CuNArray.from_numpy(x)
+    oi = ora.I32
+    assert np.array_equal(X.argmax(axis=axis).to_narr(), ora.reduce(ora.RED_ARGMAX, x, axis, oi))
+    assert np.array_equal(X.argmin(axis=axis).to_narr(), ora.reduce(ora.RED_ARGMIN, x, axis, oi))
+    bits = np.uint64 if dt == np.float64 else np.uint32
+    assert np.array_equal(X.max(axis=axis).to_narr().view(bits), ora.reduce(ora.RED_MAX, x, axis).view(bits))
+    assert np.array_equal(X.min(axis=axis).to_narr().view(bits), ora.reduce(ora.RED_MIN, x, axis).view(bits))

@@ -189,8 +189,9 @@ def test_random_expressions_match_the_python_compiler(exe):
 
 @pytest.mark.parametrize("std", ["c++17", "c++20"])
 def test_public_surface_compiles_without_warnings(std):
-    """tests/host_cpp_api.cpp uses the surface INTEGRATION.md documents; its
-    static assertions pin Crystal's result types of fused chains."""
+    """tests/host_cpp_api.cpp uses the C++ host mirror's public surface as a
+    caller does; its static assertions pin Crystal's result types of fused
+    chains."""
     gxx = shutil.which("g++")
     if not gxx:
         pytest.skip("g++ not available")
