@@ -32,7 +32,7 @@ def _random_chain(rng, shape):
     chain = []
     cur = list(shape)
     for _ in range(int(rng.integers(1, 4))):
-        k = int(rng.integers(0, 3))
+        k = int(rng.integers(0, 4))
         if k == 0 and all(c > 0 for c in cur):
             lits = []
             for n in cur:
@@ -47,8 +47,21 @@ def _random_chain(rng, shape):
             order = [int(x) for x in rng.permutation(len(cur))]
             chain.append(("permute", order))
             cur = [cur[o] for o in order]
-        else:
+        elif k == 2:
             chain.append(("reverse",))
+        else:
+            # View#reshape: a random factorisation of the element count (an
+            # affine fold where the layout allows it, a materialised copy else)
+            n = int(np.prod(cur)) if cur else 1
+            new = []
+            for _ in range(int(rng.integers(1, 4)) - 1):
+                divs = [d for d in range(1, n + 1) if n % d == 0]
+                d = divs[int(rng.integers(0, len(divs)))]
+                new.append(d)
+                n //= d
+            new.append(n)
+            chain.append(("reshape", new))
+            cur = new
     return chain
 
 
@@ -431,4 +444,27 @@ def test_integer_power_by_scalar(cu, ora):
         cu.CuNArray.from_numpy(np.array([46341, 2], np.int32)) ** 2
     with pytest.raises(ValueError):
         X ** -2
+    cu.check_errors()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.int32, np.float64, np.int64, np.bool_])
+def test_set_element(cu, dtype):
+    """MultiWritable#unsafe_set_element through set_element (negative
+    coordinates canonicalised as the reference's CoordUtil does); the other
+    elements keep their values; out-of-range and rank errors raise."""
+    rng = np.random.default_rng(3)
+    base = (rng.standard_normal([5, 7, 3]) * 50).astype(dtype)
+    X = cu.CuNArray.from_numpy(base)
+    exp = base.copy()
+    for coord in ([0, 0, 0], [4, 6, 2], [-1, 3, -2], [2, -7, 1]):
+        val = dtype(1) if dtype == np.bool_ else dtype(-17)
+        X.set_element(coord, val)
+        exp[tuple(coord)] = val
+    assert np.array_equal(X.to_narr(), exp)
+    with pytest.raises(IndexError):
+        X.set_element([5, 0, 0], dtype(1))
+    with pytest.raises(IndexError):
+        X.set_element([0, -8, 0], dtype(1))
+    with pytest.raises(cu.DimensionError):
+        X.set_element([0, 0], dtype(1))
     cu.check_errors()
