@@ -242,9 +242,12 @@ __device__ __forceinline__ void ext_parts(T v, double& d, long long& l) {
 }
 
 // Finishes one output from its accumulated result (S == 1) or stores a partial.
+// An extremum needs the output's first element (the NaN-first rule); a body
+// that already loaded it passes it as first_v with known_first set.
 template <typename T, int KIND>
 __device__ __forceinline__ void finish(const RedArgs& a, int64_t o, int64_t split, const SumAcc<T>& sacc,
-                                       const ExtAcc<T>& eacc, uint32_t& st) {
+                                       const ExtAcc<T>& eacc, uint32_t& st, bool known_first = false,
+                                       T first_v = T(0)) {
   if (a.S > 1) {
     Partial& P = a.partial[split * a.O + o];
     if (KIND == RK_SUM) {
@@ -282,7 +285,7 @@ __device__ __forceinline__ void finish(const RedArgs& a, int64_t o, int64_t spli
     long long idx = eacc.i;
     T v = eacc.v;
     // first element NaN (or no candidate): the scan never moves off element 0
-    const T first = ld<T>(a.in + out_offset(a, (uint32_t)o) * sizeof(T));
+    const T first = known_first ? first_v : ld<T>(a.in + out_offset(a, (uint32_t)o) * sizeof(T));
     if (idx < 0 || Lim<T>::nan(first)) {
       idx = 0;
       v = first;
@@ -467,6 +470,30 @@ __device__ __forceinline__ void block_extreme_into(ExtAcc<T>& acc, const T (&x)[
   acc.add(val, k + (int64_t)(j / VN) * stride + (j % VN), is_max);
 }
 
+// Folds output e of NF vectors loaded at consecutive reduced positions
+// k .. k + NF - 1 (x[j][e] is element k + j of output e) into its extremum
+// accumulator: the extreme m over the non-NaN elements, then the first j with
+// x[j][e] == m, offered once (zeros take their sign from that element), which
+// is what a strict-comparison scan skipping NaNs keeps.
+template <typename T, int NF, int VN>
+__device__ __forceinline__ void column_extreme_into(ExtAcc<T>& acc, const T (&x)[NF][VN], int e, int64_t k,
+                                                    bool is_max) {
+  T m = x[0][e];
+#pragma unroll
+  for (int j = 1; j < NF; j++) m = Lim<T>::ext(m, x[j][e], is_max);
+  int jj = -1;
+#pragma unroll
+  for (int j = NF - 1; j >= 0; j--) jj = (x[j][e] == m) ? j : jj;
+  if (jj < 0) return;  // every element NaN
+  T val = m;
+  if (m == (T)0) {
+#pragma unroll
+    for (int j = 0; j < NF; j++)
+      if (j == jj) val = x[j][e];
+  }
+  acc.add(val, k + jj, is_max);
+}
+
 // GROUP with 16-byte loads along a contiguous reduced axis: lane l of a group
 // of G reads vectors l, l + G, l + 2G, ... of each of NO outputs (elements of
 // one accumulator arrive in increasing k), then the < VN elements past the last
@@ -570,6 +597,10 @@ __device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t
     sacc[e].init();
     eacc[e].init();
   }
+  // element k = 0 of each output, kept from the first batch of split 0 so
+  // that finishing an extremum needs no further load
+  T first[VN] = {};
+  bool have_first = false;
   int64_t k = k0;
   if (a.krank == 1) {
     const int64_t ks = a.kinner * (int64_t)sizeof(T);
@@ -579,13 +610,25 @@ __device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t
       T x[NF][VN];
 #pragma unroll
       for (int j = 0; j < NF; j++) ld16<T>(p + j * ks, x[j]);
+      if constexpr (KIND != RK_SUM) {
+        if (k == 0) {
 #pragma unroll
-      for (int j = 0; j < NF; j++)
-#pragma unroll
-        for (int e = 0; e < VN; e++) {
-          if (KIND == RK_SUM) sacc[e].add(x[j][e]);
-          else eacc[e].add(x[j][e], k + j, is_max);
+          for (int e = 0; e < VN; e++) first[e] = x[0][e];
+          have_first = true;
         }
+      }
+      if constexpr (KIND != RK_SUM && sizeof(T) == 4) {
+#pragma unroll
+        for (int e = 0; e < VN; e++) column_extreme_into<T, NF, VN>(eacc[e], x, e, k, is_max);
+      } else {
+#pragma unroll
+        for (int j = 0; j < NF; j++)
+#pragma unroll
+          for (int e = 0; e < VN; e++) {
+            if (KIND == RK_SUM) sacc[e].add(x[j][e]);
+            else eacc[e].add(x[j][e], k + j, is_max);
+          }
+      }
     }
     for (; k < k1; k++, p += ks) {
       T x[VN];
@@ -608,7 +651,7 @@ __device__ __forceinline__ void column_vec(const RedArgs& a, int64_t o0, int64_t
     }
   }
 #pragma unroll
-  for (int e = 0; e < VN; e++) finish<T, KIND>(a, o0 + e, split, sacc[e], eacc[e], st);
+  for (int e = 0; e < VN; e++) finish<T, KIND>(a, o0 + e, split, sacc[e], eacc[e], st, have_first, first[e]);
 }
 
 // SLAB: the reduced axis sits directly outside the innermost kept axis and
