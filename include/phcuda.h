@@ -331,9 +331,12 @@ typedef struct {
  * other; buffers must outlive the handle. */
 PHCU_API int32_t phcu_batch_prepare(const phcu_task_t* tasks, int32_t n_tasks, const phcu_program_t* programs,
                                     int32_t n_programs, void** batch);
-/* mode 0: one persistent launch over the device work queue; mode 1: one
- * ordinary launch per task (the per-op baseline); mode 2: the per-op launches
- * captured once in a CUDA graph and replayed. */
+/* mode 0: the persistent launches over the device work queue, one per body
+ * class present (tasks grouped by kernel kind), side by side: the first on
+ * the library stream, the others on side streams forked from it, which the
+ * library stream then waits for, so later work on it sees every result;
+ * mode 1: one ordinary launch per task (the per-op baseline); mode 2: the
+ * per-op launches captured once in a CUDA graph and replayed. */
 PHCU_API int32_t phcu_batch_launch(void* batch, int32_t mode);
 /* Planned task count (empty tasks dropped), work items and algorithmic bytes. */
 PHCU_API int32_t phcu_batch_info(void* batch, int64_t* n_tasks, int64_t* n_items, int64_t* bytes);

@@ -323,9 +323,23 @@ int32_t batch_launch(Batch* b, int mode) {
   if (mode == 0) {
     PHCU_CUDA(cudaMemsetAsync(b->d_ticket, 0, BC_COUNT * sizeof(unsigned long long), s));
     if (b->n_counters) PHCU_CUDA(cudaMemsetAsync(b->d_counters, 0, b->n_counters * sizeof(uint32_t), s));
+    // The class kernels run side by side: the first on the library stream,
+    // each later one on a side stream forked from it, all joined back.  Each
+    // fills the GPU, so a later class mostly takes over SMs as the earlier
+    // classes' blocks run out of items (10,000 uneven tasks: 2.00 -> 1.91 ms;
+    // a fixed split of blocks per SM between the classes ran 2.4-3.6 ms).
+    Context& c = ctx();
+    PHCU_CUDA(cudaEventRecord(c.ev_fork, s));  // after the memsets, before the first class
+    int nside = 0;
+    bool first = true;
     for (int cls = 0; cls < BC_COUNT; cls++) {
       const Phase& ph = b->phases[cls];
       if (!ph.kernel) continue;
+      cudaStream_t ls = s;
+      if (!first) {
+        ls = c.side[nside];
+        PHCU_CUDA(cudaStreamWaitEvent(ls, c.ev_fork, 0));
+      }
       BatchArgs A;
       A.tasks = b->d_tasks;
       A.item_task = b->d_item_task;
@@ -336,10 +350,21 @@ int32_t batch_launch(Batch* b, int mode) {
       A.item_begin = ph.begin;
       A.item_end = ph.end;
       A.deadline_ns = 20ull * 1000 * 1000 * 1000;  // 20 s
-      ph.kernel<<<ph.grid, BATCH_THREADS, ph.smem, s>>>(A);
+      ph.kernel<<<ph.grid, BATCH_THREADS, ph.smem, ls>>>(A);
       count_launch();
-      PHCU_TRY(check_launch("batch_kernel"));
+      int32_t rc = check_launch("batch_kernel");
+      if (!first && rc == PHCU_OK) {
+        const cudaError_t e = cudaEventRecord(c.ev_join[nside], ls);
+        if (e == cudaSuccess) nside++;
+        else rc = cuda_fail(e, "cudaEventRecord(batch join)");
+      }
+      first = false;
+      if (rc != PHCU_OK) {  // join what was forked, then report
+        for (int i = 0; i < nside; i++) cudaStreamWaitEvent(s, c.ev_join[i], 0);
+        return rc;
+      }
     }
+    for (int i = 0; i < nside; i++) PHCU_CUDA(cudaStreamWaitEvent(s, c.ev_join[i], 0));
     return PHCU_OK;
   }
   if (mode == 2 && b->graph && b->graph_stream == s) {

@@ -49,6 +49,12 @@ struct Context {
   // copy direction, so both copy engines and the SMs work at once)
   cudaStream_t d2h = nullptr, h2d = nullptr;
   cudaEvent_t ev_work = nullptr, ev_h2d = nullptr;
+  // side streams of a batch launch: its class kernels after the first run
+  // beside it, forked from and joined back to the library stream by events
+  static constexpr int NSIDE = 4;
+  cudaStream_t side[NSIDE] = {};
+  cudaEvent_t ev_fork = nullptr;
+  cudaEvent_t ev_join[NSIDE] = {};
 };
 Context& ctx();
 int32_t require_ctx();

@@ -100,6 +100,8 @@ static void release_context(Context& c) {
   if (c.own_stream) cudaStreamSynchronize(c.own_stream);
   if (c.d2h) cudaStreamSynchronize(c.d2h);
   if (c.h2d) cudaStreamSynchronize(c.h2d);
+  for (int i = 0; i < Context::NSIDE; i++)
+    if (c.side[i]) cudaStreamSynchronize(c.side[i]);
   release_heat_graphs();
   release_noalloc_scratch();
   if (c.l2_scrub) cudaFree(c.l2_scrub);
@@ -108,6 +110,11 @@ static void release_context(Context& c) {
   if (c.ev_h2d) cudaEventDestroy(c.ev_h2d);
   if (c.d2h) cudaStreamDestroy(c.d2h);
   if (c.h2d) cudaStreamDestroy(c.h2d);
+  for (int i = 0; i < Context::NSIDE; i++) {
+    if (c.ev_join[i]) cudaEventDestroy(c.ev_join[i]);
+    if (c.side[i]) cudaStreamDestroy(c.side[i]);
+  }
+  if (c.ev_fork) cudaEventDestroy(c.ev_fork);
   if (c.own_stream) cudaStreamDestroy(c.own_stream);
   c = Context();
   g_nocc = 0;  // attributes and occupancy belong to this device's context
@@ -138,6 +145,11 @@ static int32_t create_context(Context& c, int32_t device) {
   PHCU_CUDA(cudaStreamCreateWithFlags(&c.h2d, cudaStreamNonBlocking));
   PHCU_CUDA(cudaEventCreateWithFlags(&c.ev_work, cudaEventDisableTiming));
   PHCU_CUDA(cudaEventCreateWithFlags(&c.ev_h2d, cudaEventDisableTiming));
+  PHCU_CUDA(cudaEventCreateWithFlags(&c.ev_fork, cudaEventDisableTiming));
+  for (int i = 0; i < Context::NSIDE; i++) {
+    PHCU_CUDA(cudaStreamCreateWithFlags(&c.side[i], cudaStreamNonBlocking));
+    PHCU_CUDA(cudaEventCreateWithFlags(&c.ev_join[i], cudaEventDisableTiming));
+  }
   c.device = device;
   c.launches = 0;
   c.ready = true;

@@ -62,6 +62,40 @@ def test_batch_modes_match_oracle(cu, ora, small_workload, mode):
     b.close()
 
 
+def test_persistent_batch_replays_from_a_graph(cu, small_workload):
+    """A persistent launch runs its class kernels side by side: the first on
+    the library stream, the others on side streams forked from it and joined
+    back.  The fork and the join hold inside a stream capture too, so the
+    launch captured once (phcu_graph_begin/end) and replayed gives the
+    results of a direct launch."""
+    import ctypes
+
+    from phase_cu import _abi
+    from phase_cu.batch import Batch
+
+    wl = small_workload
+    lib = _abi.load()
+    b = Batch(wl.tasks(), wl.programs)
+    _abi.call("phcu_memset", wl.out.ptr, 0, wl.out.nbytes)
+    b.launch(0)
+    cu.check_errors()
+    ref = wl.download_outputs()
+    g = ctypes.c_void_p()
+    _abi.check(lib.phcu_graph_begin())
+    b.launch(0)
+    _abi.check(lib.phcu_graph_end(ctypes.byref(g)))
+    try:
+        _abi.call("phcu_memset", wl.out.ptr, 0, wl.out.nbytes)
+        for _ in range(2):
+            _abi.check(lib.phcu_graph_launch(g))
+        cu.check_errors()
+        got = wl.download_outputs()
+    finally:
+        lib.phcu_graph_destroy(g)
+        b.close()
+    assert np.array_equal(got, ref)
+
+
 def test_batch_configs_do_not_change_results(cu, small_workload):
     from phase_cu import _abi
     from phase_cu.batch import Batch
