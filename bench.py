@@ -470,12 +470,12 @@ def e2e_leg(A, lib, arrays, dev_arrays, jobs, args, timer, stop, step_bytes):
 
     run_steps(dev_arrays, 1)
     A.call("phcu_sync")
-    # three rounds of up to five steps each, the median round reported: the
+    # five rounds of up to five steps each, the median round reported: the
     # host link is shared with the rest of the machine, and one round alone
     # has ranged from 35 to 56 ms per step on the same box
     steps = max(1, min(args.steps, 5))
     rounds = []
-    for _ in range(3):
+    for _ in range(5):
         t = timer()
         run_steps(dev_arrays, steps)
         rounds.append(stop(t) / steps)

@@ -255,23 +255,16 @@ static __device__ __noinline__ void tma_issue(const EvalTmaArgs& T, uint64_t tt,
 // staged input, 16 KB per input).  Copies keep three tiles in flight per
 // block (four stages, 65 KB, three blocks per SM): the permuted gather of
 // 512x512x256 Float32 took 86.9 us instead of 94.6 with two stages and
-// 95.2 with three.  Kernels with two staged inputs keep two stages and
-// three blocks per SM: three stages leave two blocks, and the permuted
-// binary then took 143.7 us instead of 127.5 (the Int32 division 275.9
-// instead of 235.3).  At most three stages where four inputs can be staged:
+// 95.2 with three.  The Int32 / Int32 -> Float64 division, bound by its
+// arithmetic, takes one stage (33 KB) so that four blocks fit instead of
+// three: 230.9 us instead of 235.1.  Other kernels with two staged inputs
+// keep two stages and three blocks per SM: three stages leave two blocks,
+// and the permuted binary then took 143.7 us instead of 127.5 (the
+// division 275.9).  At most three stages where four inputs can be staged:
 // 3 x 4 x 16 KB + 1 KB stays under the 227 KB a block may use.
-#ifndef PHCU_TMA_NST_COPY
-#define PHCU_TMA_NST_COPY 4
-#endif
-#ifndef PHCU_TMA_NST_32
-#define PHCU_TMA_NST_32 2
-#endif
-#ifndef PHCU_TMA_NST_64
-#define PHCU_TMA_NST_64 2
-#endif
 template <typename S, int FAST>
 constexpr int tma_stages() {
-  return FAST == FAST_COPY ? PHCU_TMA_NST_COPY : (sizeof(S) == 8 ? PHCU_TMA_NST_64 : PHCU_TMA_NST_32);
+  return FAST == FAST_COPY ? 4 : (FAST == FAST_IDIV ? 1 : 2);
 }
 
 // Persistent over tiles t = blockIdx.x + i * gridDim.x with an NST-stage
