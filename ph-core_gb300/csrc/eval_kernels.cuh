@@ -31,9 +31,16 @@ constexpr int min_blocks() {
 // 16 elements at four blocks: 145; 32 at two: 200).  The ROW kernel of a
 // pre-decoded 32-bit program fits 64 registers without spills: four resident
 // blocks instead of three (fused chain 220 -> 187 us).
-template <typename S, int FAST>
+// The ROW Int32 / Int32 -> Float64 division over 8-element chunks fits 48
+// registers without spills at five blocks per SM: 206 us instead of 221 at
+// four on the reversed 512x512x256 views (the TMA division spills at five
+// and keeps four; six blocks spill the ROW one too).
+template <typename S, int FAST, int VEC>
 constexpr int row_min_blocks() {
-  return (FAST == FAST_BINOP && sizeof(S) == 4) ? 4 : (FAST == FAST_FX && sizeof(S) == 4) ? 4 : min_blocks<FAST>();
+  return (FAST == FAST_BINOP && sizeof(S) == 4) ? 4
+         : (FAST == FAST_FX && sizeof(S) == 4)  ? 4
+         : (FAST == FAST_IDIV && VEC == 8)      ? 5
+                                                : min_blocks<FAST>();
 }
 
 // ROW: each thread handles U grid-strided chunks of VEC elements per iteration.
@@ -41,7 +48,7 @@ constexpr int row_min_blocks() {
 // reads one instruction per step at a run-time index, which shared memory
 // serves with one vector load (kernel-parameter space would serialise it).
 template <typename S, int NIN, int VEC, int U, bool STASH, int FAST>
-__global__ void __launch_bounds__(ROW_THREADS, row_min_blocks<S, FAST>())
+__global__ void __launch_bounds__(ROW_THREADS, row_min_blocks<S, FAST, VEC>())
     eval_row_kernel(const __grid_constant__ EvalArgs A) {
   const uint32_t nchunks = (uint32_t)(A.plan.sp.n / VEC);
   const uint32_t nthreads = gridDim.x * blockDim.x;
