@@ -121,6 +121,22 @@ struct DType<int64_t> {
   static constexpr const char* name = "Int64";
 };
 
+// Crystal's Bool as a one-byte device element: the result of the elementwise
+// comparisons and the mask of masked writes.  (std::vector<bool> packs bits,
+// so host copies of Bool arrays use this one-byte type instead.)
+struct Bool {
+  uint8_t v = 0;
+  Bool() = default;
+  Bool(bool b) : v(b ? 1 : 0) {}
+  operator bool() const { return v != 0; }
+};
+static_assert(sizeof(Bool) == 1, "Bool is one byte on the device");
+template <>
+struct DType<Bool> {
+  static constexpr int32_t id = PHCU_BOOL;
+  static constexpr const char* name = "Bool";
+};
+
 // -------------------------------------------------------- region literals
 // One entry of a region literal: an integer index (the axis is dropped) or a
 // Crystal range `first..last`, `first...last`, `first..step..last` with any of
@@ -583,6 +599,15 @@ class CuView {
   Affine aff_;
 };
 
+namespace detail {
+// defined with the fused expressions below
+inline std::string shape_text(const std::vector<int64_t>& s);
+inline int64_t slot_bits(float v);
+inline int64_t slot_bits(double v);
+inline int64_t slot_bits(int32_t v);
+inline int64_t slot_bits(int64_t v);
+}  // namespace detail
+
 // A device-resident NArray (src/n_array.cr): one row-major buffer.  Copies of
 // a CuNArray share the buffer, as Crystal references to one NArray do;
 // clone() makes an independent copy (NArray#clone, n_array.cr:372-374).
@@ -635,6 +660,44 @@ class CuNArray : public CuView<T> {
   // aliases the region in another element order is refused.
   void set_chunk(const std::vector<Lit>& region, const CuProcView<T>& src);
 
+  // MultiIndexable#get / #unsafe_fetch_element (multi_indexable.cr, n_array.cr:456-458)
+  // and MultiWritable#set_element / #unsafe_set_element (n_array.cr:503-505):
+  // one element, negative indices counted from the end (CoordUtil).  Slow
+  // paths: one download or one fill per element.
+  T get(const std::vector<int64_t>& coord) const { return this->view(coord_lits(coord)).to_vector()[0]; }
+  void set_element(const std::vector<int64_t>& coord, T value) { set_chunk(coord_lits(coord), value); }
+
+  // MultiIndexable#slices / #each_slice (multi_indexable.cr:742-786): the
+  // chunks with axis `axis` fixed at 0, 1, ... and dropped.
+  std::vector<CuNArray> slices(int axis = 0) const {
+    const int d = (int)this->dimensions();
+    if (axis < 0 || axis >= d)
+      throw IndexError("axis " + std::to_string(axis) + " is not present in a " + std::to_string(d) +
+                       "-dimensional MultiIndexable");
+    std::vector<CuNArray> out;
+    for (int64_t i = 0; i < this->shape()[axis]; i++) {
+      std::vector<Lit> lits((size_t)d, all());
+      lits[(size_t)axis] = idx(i);
+      out.push_back(get_chunk(lits));
+    }
+    return out;
+  }
+
+  // NArray#[]=(mask, value) and MultiWritable#set_mask (n_array.cr:510-551,
+  // multi_writable.cr:127-172): value, or the element of src, wherever mask
+  // holds true; one in-place select kernel.
+  void set_mask(const CuView<Bool>& mask, T value) { masked_write(mask, nullptr, value); }
+  void set_mask(const CuView<Bool>& mask, const CuView<T>& src) { masked_write(mask, &src, T(0)); }
+
+  // Mutable#map! (mutable.cr:29-33, n_array.cr:621-627): self = f(self), and
+  // Mutable#map_with! (mutable.cr:54-67): self = f(self, other), each one
+  // program written into the array itself.  The block returns a Sym of the
+  // array's element type.
+  template <typename F>
+  CuNArray& map_inplace(F f);
+  template <typename U, typename F>
+  CuNArray& map_with_inplace(const CuView<U>& other, F f);
+
  private:
   static int64_t count(const std::vector<int64_t>& shape) {
     for (int64_t s : shape)
@@ -656,6 +719,47 @@ class CuNArray : public CuView<T> {
     else s.v.i = (int64_t)value;
     check(phcu_fill(&v, &s), "phcu_fill");
   }
+  std::vector<Lit> coord_lits(const std::vector<int64_t>& coord) const {
+    if (coord.size() != this->dimensions())
+      throw DimensionError("Could not canonicalize coordinate " + detail::shape_text(coord) + " to fit in shape " +
+                           detail::shape_text(this->shape()));
+    std::vector<Lit> lits;
+    for (int64_t c : coord) lits.push_back(idx(c));
+    return lits;
+  }
+  // Program: S0 = mask; ACC = self; ACC = S0 ? source : ACC, with the source
+  // an input view or the value as an immediate; inputs {mask, source, self}.
+  void masked_write(const CuView<Bool>& mask, const CuView<T>* src, T value) {
+    if (mask.shape() != this->shape())
+      throw ShapeError("Cannot perform masking: mask shape " + detail::shape_text(mask.shape()) +
+                       " does not match array shape " + detail::shape_text(this->shape()) + ".");
+    if (src && src->shape() != this->shape())
+      throw ShapeError("Cannot perform masking: source shape " + detail::shape_text(src->shape()) +
+                       " does not match array shape " + detail::shape_text(this->shape()) + ".");
+    if (src) refuse_reordered_alias(*this, src->buffer().get(), src->layout());
+    phcu_program_t p;
+    std::memset(&p, 0, sizeof(p));
+    const int32_t t = DType<T>::id;
+    auto emit = [&p](int32_t op, int32_t sr, int32_t ty, int32_t bt, int64_t imm) {
+      phcu_instr_t& c = p.code[p.n_instr++];
+      c.op = (uint8_t)op;
+      c.src = (uint8_t)sr;
+      c.type = (uint8_t)ty;
+      c.btype = (uint8_t)bt;
+      c.imm.i = imm;
+    };
+    emit(PHCU_I_LD, 0, PHCU_BOOL, PHCU_BOOL, 0);
+    emit(PHCU_I_ST0, 0, PHCU_BOOL, 0, 0);
+    emit(PHCU_I_LD, 2, t, t, 0);
+    if (src) emit(PHCU_I_SEL, 1, t, t, 0);
+    else emit(PHCU_I_SEL, PHCU_SRC_IMM, t, t, detail::slot_bits(value));
+    p.out_type = t;
+    const phcu_view_t me = this->desc();
+    phcu_view_t ins[3] = {mask.desc(), src ? src->desc() : me, me};
+    check(phcu_eval(&p, ins, 3, &me), "phcu_eval");
+  }
+  template <typename R>
+  void write_self(const CuProcView<R>& pv);
 };
 
 template <typename T>
@@ -750,6 +854,45 @@ template <typename T>
 CuNArray<T> wsub(const CuView<T>& a, const CuView<T>& b) { return detail::binary<T>(PHCU_OP_WSUB, a, b); }
 template <typename T>
 CuNArray<T> wmul(const CuView<T>& a, const CuView<T>& b) { return detail::binary<T>(PHCU_OP_WMUL, a, b); }
+
+// The elementwise comparisons > < >= <= and #eq (multi_indexable.cr:899-913):
+// Bool arrays, the masks of set_mask.
+template <typename T>
+CuNArray<Bool> gt(const CuView<T>& a, const CuView<T>& b) { return detail::binary<Bool>(PHCU_OP_GT, a, b); }
+template <typename T>
+CuNArray<Bool> lt(const CuView<T>& a, const CuView<T>& b) { return detail::binary<Bool>(PHCU_OP_LT, a, b); }
+template <typename T>
+CuNArray<Bool> ge(const CuView<T>& a, const CuView<T>& b) { return detail::binary<Bool>(PHCU_OP_GE, a, b); }
+template <typename T>
+CuNArray<Bool> le(const CuView<T>& a, const CuView<T>& b) { return detail::binary<Bool>(PHCU_OP_LE, a, b); }
+template <typename T>
+CuNArray<Bool> eq(const CuView<T>& a, const CuView<T>& b) { return detail::binary<Bool>(PHCU_OP_EQ, a, b); }
+
+// MultiIndexable#equals? / #== (multi_indexable.cr:74-84, 871-879): same shape
+// and equal elements.  The comparison, a Bool -> Int32 conversion and the
+// minimum run on the device; one Int32 comes back.
+template <typename T>
+bool equals(const CuView<T>& a, const CuView<T>& b) {
+  if (a.shape() != b.shape()) return false;
+  if (a.size() == 0) return true;
+  const CuNArray<Bool> same = eq(a, b);
+  CuNArray<int32_t> flags(a.shape());
+  phcu_program_t p;
+  std::memset(&p, 0, sizeof(p));
+  p.n_instr = 2;
+  p.out_type = PHCU_I32;
+  p.code[0].op = PHCU_I_LD;
+  p.code[0].type = p.code[0].btype = PHCU_BOOL;
+  p.code[1].op = PHCU_I_CVT;
+  p.code[1].type = p.code[1].btype = PHCU_BOOL;
+  p.code[1].imm.i = PHCU_I32;
+  const phcu_view_t in = same.desc(), o = flags.desc();
+  check(phcu_eval(&p, &in, 1, &o), "phcu_eval");
+  CuNArray<int32_t> m(std::vector<int64_t>{1});
+  const phcu_view_t fv = flags.desc(), mv = m.desc();
+  check(phcu_reduce(PHCU_RED_MIN, &fv, -1, &mv), "phcu_reduce");
+  return m.to_vector()[0] == 1;
+}
 
 // ---------------------------------------------------- fused expressions
 // ProcView (src/proc_view.cr:6-35) and chained infix operators build an
@@ -1204,6 +1347,12 @@ class CuProcView {
   // One phcu_eval into a new contiguous array (more than one when the
   // expression is larger than one device program: see detail::split_to_fit).
   CuNArray<T> to_cu() const {
+    CuNArray<T> out(shape_);
+    eval_into(out.desc());
+    return out;
+  }
+  // The same into an existing view of this shape (an in-place map).
+  void eval_into(const phcu_view_t& o) const {
     bool raises = false;
     std::vector<detail::Leaf> leaves = leaves_;
     detail::ExprP expr = expr_;
@@ -1211,14 +1360,11 @@ class CuProcView {
     bool r = false;
     const phcu_program_t p = detail::compile_program(expr, DType<T>::id, &r);
     raises = raises || r;
-    CuNArray<T> out(shape_);
     phcu_view_t ins[PHCU_MAX_INPUTS];
     std::memset(ins, 0, sizeof(ins));
     for (size_t k = 0; k < leaves.size(); k++) ins[k] = leaves[k].desc();
-    const phcu_view_t o = out.desc();
     check(phcu_eval(&p, ins, (int32_t)leaves.size(), &o), "phcu_eval");
     if (raises) check_status();
-    return out;
   }
   std::vector<T> to_vector() const { return to_cu().to_vector(); }
   // MultiIndexable#get_chunk: evaluates the region's elements only.
@@ -1235,6 +1381,39 @@ void CuNArray<T>::set_chunk(const std::vector<Lit>& region, const CuProcView<T>&
   const CuView<T> dst = this->view(region);
   for (const detail::Leaf& l : src.leaves()) refuse_reordered_alias(dst, l.buf.get(), l.aff);
   set_chunk(region, src.to_cu());
+}
+
+// In-place maps: the program is written into the array itself.  Every
+// operand must read the array in its own element order (the reference reads
+// and writes element by element); the array itself always does.
+template <typename T>
+template <typename R>
+void CuNArray<T>::write_self(const CuProcView<R>& pv) {
+  static_assert(std::is_same<R, T>::value, "an in-place map keeps the array's element type");
+  for (const detail::Leaf& l : pv.leaves()) refuse_reordered_alias(*this, l.buf.get(), l.aff);
+  pv.eval_into(this->desc());
+}
+
+template <typename T>
+template <typename F>
+CuNArray<T>& CuNArray<T>::map_inplace(F f) {
+  write_self(this->process(f));
+  return *this;
+}
+
+template <typename T>
+template <typename U, typename F>
+CuNArray<T>& CuNArray<T>::map_with_inplace(const CuView<U>& other, F f) {
+  if (other.shape() != this->shape())
+    throw ShapeError("The shape of this MultiIndexable (" + detail::shape_text(this->shape()) +
+                     ") does not match the shape of the one provided (" + detail::shape_text(other.shape()) + ").");
+  auto r = f(Sym<T>::input(0), Sym<U>::input(1));
+  static_assert(detail::IsSym<decltype(r)>::value, "a map_with! block returns a Sym");
+  using R = typename decltype(r)::value_type;
+  write_self(CuProcView<R>({detail::Leaf{this->buf_, this->aff_, DType<T>::id},
+                            detail::Leaf{other.buffer(), other.layout(), DType<U>::id}},
+                           r.e, this->shape()));
+  return *this;
 }
 
 template <typename T>

@@ -1,7 +1,8 @@
 // Compile-only check of the C++ host mirror's public surface
 // (ph-core_gb300/host/phase.hpp) as a caller uses it: views,
 // eager operators with Crystal's result types, fused CuProcView chains,
-// reductions, chunk reads and writes, region operations.  The static
+// reductions, chunk reads and writes, element access, slices, comparisons,
+// masked writes, equality, in-place maps, region operations.  The static
 // assertions pin the result types; tests/test_host_cpp_programs.py compiles
 // this file with warnings as errors.  Nothing here runs.
 #include <type_traits>
@@ -61,6 +62,20 @@ void api(const std::vector<float>& host_f, const std::vector<int32_t>& host_i) {
   float total = sum(chain);
   std::vector<int64_t> where = argmax(chain.permute().reverse());
 
+  // element access, slices, comparisons, masks, equality, in-place maps
+  float e0 = a.get({0, -1, 3});
+  a.set_element({1, 2, 3}, 4.0f);
+  std::vector<CuNArray<float>> sl = a.slices(2);
+  CuNArray<Bool> m = gt(a, b);
+  static_assert(same<decltype(lt(ai, bi)), CuNArray<Bool>>, "comparisons give Bool arrays");
+  std::vector<Bool> mh = m.to_vector();
+  a.set_mask(m, 0.0f);
+  a.set_mask(m, b.view({}));
+  bool eqs = equals(a, b) || equals<int32_t>(ai, bi);
+  CuNArray<float>& self = a.map_inplace([](auto e) { return e * 3 + 1; });
+  ai.map_with_inplace(bi.view({}), [](auto u, auto v) { return u - v * 2; });
+  a.map_with_inplace(ai.view({}), [](auto u, auto v) { return u * v; });  // Float32 * Int32 stays Float32
+
   // region operations
   IndexRegion reg = IndexRegion::absolute({rng(3, 20, 4), rng(7, std::nullopt, -2)});
   bool fits = reg.fits_in({21, 8});
@@ -70,5 +85,5 @@ void api(const std::vector<float>& host_f, const std::vector<int32_t>& host_i) {
   std::vector<int64_t> abs = reg.local_to_absolute({1, 2});
   reg.trim({10, 4});
   (void)i, (void)q, (void)w, (void)out, (void)s1, (void)am, (void)corner, (void)total, (void)where;
-  (void)fits, (void)has, (void)abs, (void)r;
+  (void)fits, (void)has, (void)abs, (void)r, (void)e0, (void)sl, (void)mh, (void)eqs, (void)self;
 }

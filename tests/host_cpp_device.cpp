@@ -3,7 +3,8 @@
 // given as argv[1], writes each result as <name>.bin there and prints one line
 // per result or raised exception; tests/test_gpu_host_cpp.py compares them
 // with the oracle.  With argv[2] = "proc" it runs the fused expressions
-// (CuProcView) instead of the eager operators.
+// (CuProcView) instead of the eager operators; with "more" element access,
+// slices, comparisons, masked writes, equality and in-place maps.
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -120,6 +121,49 @@ static void run_proc(const std::string& tag) {
   save(tag + "_proc_five", ((A.process() + B) * (A.view(rev).process() - B.view(rev)) + A.reverse()).to_vector());
 }
 
+// Element access, slices, comparisons, masked writes, equality and in-place maps.
+template <typename T>
+static void run_more(const std::string& tag) {
+  const std::vector<int64_t> shape = {16, 12, 10};
+  const size_t n = 16 * 12 * 10;
+  const CuNArray<T> A = CuNArray<T>::of_buffer(shape, load<T>("a." + tag, n));
+  const CuNArray<T> B = CuNArray<T>::of_buffer(shape, load<T>("b." + tag, n));
+  const std::vector<Lit> rev = {all(), rng(std::nullopt, std::nullopt, -1), all()};
+  CuNArray<T> D = A.clone();
+  D.map_inplace([](auto e) { return e * 3 + 1; });
+  save(tag + "_map_inplace", D.to_vector());
+  CuNArray<T> E = A.clone();
+  E.map_with_inplace(B.view(rev), [](auto x, auto y) { return x - y * 2; });
+  save(tag + "_map_with_inplace", E.to_vector());
+  save(tag + "_get", std::vector<T>{A.get({3, -1, 2}), A.get({-16, 0, -1})});
+  CuNArray<T> F = A.clone();
+  F.set_element({0, 0, 0}, T(42));
+  F.set_element({-1, -1, -1}, T(-7));
+  save(tag + "_set_element", F.to_vector());
+  expect_raise(tag + "_get_index", [&] { return A.get({16, 0, 0}); });
+  expect_raise(tag + "_get_dim", [&] { return A.get({1, 2}); });
+  const std::vector<CuNArray<T>> sl = A.slices(1);
+  std::cout << "nslices " << tag << " " << sl.size() << "\n";
+  save(tag + "_slice5", sl[5].to_vector());
+  const CuNArray<Bool> m = gt(A, B);
+  save(tag + "_gt", m.to_vector());
+  CuNArray<T> G = A.clone();
+  G.set_mask(m, T(0));
+  save(tag + "_mask_value", G.to_vector());
+  CuNArray<T> H = A.clone();
+  H.set_mask(m, B.view(rev));
+  save(tag + "_mask_src", H.to_vector());
+  expect_raise(tag + "_mask_shape", [&] {
+    CuNArray<T> X = A.clone();
+    X.set_mask(gt(A.permute({2, 0, 1}), B.permute({2, 0, 1})), T(1));
+    return X;
+  });
+  std::cout << "equals " << tag << " same " << equals(A, A.clone()) << "\n";
+  std::cout << "equals " << tag << " other " << equals(A, B) << "\n";
+  std::cout << "equals " << tag << " reversed " << equals(A.view(rev), A.view(rev).to_cu()) << "\n";
+  std::cout << "equals " << tag << " shape " << equals(A.view({}), A.permute({2, 0, 1})) << "\n";
+}
+
 static void run_proc_mixed() {
   const std::vector<int64_t> shape = {16, 12, 10};
   const size_t n = 16 * 12 * 10;
@@ -136,6 +180,17 @@ static void run_proc_mixed() {
 int main(int argc, char** argv) {
   if (argc < 2) return 2;
   dir = argv[1];
+  if (argc > 2 && std::string(argv[2]) == "more") {
+    try {
+      init(0);
+      run_more<float>("f32");
+      run_more<int32_t>("i32");
+    } catch (const std::exception& e) {
+      std::cout << "error " << e.what() << "\n";
+      return 1;
+    }
+    return 0;
+  }
   if (argc > 2 && std::string(argv[2]) == "proc") {
     try {
       init(0);

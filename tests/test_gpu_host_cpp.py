@@ -1,6 +1,7 @@
 """The C++ host mirror (ph-core_gb300/host/phase.hpp) on the device: views,
 infix operators with Crystal's result types, fused chains (CuProcView: one
-program per materialisation), reductions, chunk reads and writes and the
+program per materialisation), reductions, chunk reads and writes, element
+access, slices, comparisons, masked writes, equality, in-place maps and the
 reference's exceptions, checked against the oracle on 16x12x10 Float32 and
 Int32 arrays (bit-exact; sums within 1e-6 relative of the FP64 oracle)."""
 import os
@@ -76,6 +77,47 @@ def run(built):
 @pytest.fixture(scope="module")
 def run_proc(built):
     return _drive(built, "proc")
+
+
+@pytest.fixture(scope="module")
+def run_more(built):
+    return _drive(built, "more")
+
+
+@pytest.mark.parametrize("tag", ["f32", "i32"])
+def test_element_access_slices_masks_equality_and_inplace_maps(run_more, ora, cu, tag):
+    """get / set_element, slices(axis), the elementwise comparison as a Bool
+    array, set_mask with a value and with a source view, equals? and the
+    in-place maps map! and map_with! of the C++ mirror, against the oracle
+    (bit-exact)."""
+    arrays, lines, load = run_more
+    a, b = arrays[tag]
+    dt = a.dtype
+    rb = np.ascontiguousarray(b[:, ::-1, :])
+    m, _ = ora.map_binary_scalar(ora.OP_MUL, a, 3, ora.I32)
+    m, _ = ora.map_binary_scalar(ora.OP_ADD, m, 1, ora.I32)
+    assert m.dtype == dt
+    assert np.array_equal(load(tag + "_map_inplace", dt), m.reshape(-1))
+    w, _ = ora.map_binary_scalar(ora.OP_MUL, rb, 2, ora.I32)
+    w, _ = ora.map_binary(ora.OP_SUB, a, w)
+    assert np.array_equal(load(tag + "_map_with_inplace", dt), w.reshape(-1))
+    assert np.array_equal(load(tag + "_get", dt), np.array([a[3, -1, 2], a[-16, 0, -1]], dtype=dt))
+    f = a.copy()
+    f[0, 0, 0] = 42
+    f[-1, -1, -1] = -7
+    assert np.array_equal(load(tag + "_set_element", dt), f.reshape(-1))
+    assert "raised %s_get_index IndexError" % tag in lines
+    assert "raised %s_get_dim DimensionError" % tag in lines
+    assert "nslices %s 12" % tag in lines
+    assert np.array_equal(load(tag + "_slice5", dt), ora.narray_fetch_chunk(a, [slice(None), 5]).reshape(-1))
+    gt, _ = ora.map_binary(ora.OP_GT, a, b)
+    mask = np.asarray(gt).reshape(-1).astype(bool)
+    assert np.array_equal(load(tag + "_gt", np.uint8).astype(bool), mask)
+    assert np.array_equal(load(tag + "_mask_value", dt), np.where(mask, dt.type(0), a.reshape(-1)))
+    assert np.array_equal(load(tag + "_mask_src", dt), np.where(mask, rb.reshape(-1), a.reshape(-1)))
+    assert "raised %s_mask_shape ShapeError" % tag in lines
+    for what, expected in (("same", 1), ("other", 0), ("reversed", 1), ("shape", 0)):
+        assert "equals %s %s %d" % (tag, what, expected) in lines
 
 
 @pytest.mark.parametrize("tag", ["f32", "i32"])
