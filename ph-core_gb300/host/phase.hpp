@@ -551,6 +551,51 @@ inline Affine affine_reverse(const Affine& a) {
   return r;
 }
 
+// ReshapeTransform (transforms.cr:118-189) as strides, when the view's layout
+// allows it: the lexicographic order is regrouped without moving elements.
+// Empty when the new shape cannot be expressed with strides.
+inline std::optional<Affine> affine_reshape(const Affine& a, const std::vector<int64_t>& ns) {
+  if (shape_to_size(ns) == 0 || shape_to_size(a.shape) == 0) return Affine{a.offset, ns, row_major(ns)};
+  std::vector<std::pair<int64_t, int64_t>> old;  // (extent, stride) of the axes longer than 1
+  for (size_t i = 0; i < a.shape.size(); i++)
+    if (a.shape[i] != 1) old.push_back({a.shape[i], a.stride[i]});
+  std::vector<int64_t> nst(ns.size(), 0);
+  size_t oi = 0, ni = 0;
+  const size_t on = old.size(), nn = ns.size();
+  while (ni < nn && oi < on) {
+    if (ns[ni] == 1) {
+      nst[ni++] = 0;
+      continue;
+    }
+    // old axes [oi, oj) and new axes [ni, nj) of equal element count
+    int64_t op = old[oi].first, np = ns[ni];
+    size_t oj = oi + 1, nj = ni + 1;
+    while (op != np) {
+      if (op < np) {
+        if (oj >= on) return std::nullopt;
+        op *= old[oj++].first;
+      } else {
+        if (nj >= nn) return std::nullopt;
+        np *= ns[nj++];
+      }
+    }
+    for (size_t k = oi; k + 1 < oj; k++)  // the old group must be contiguous in itself
+      if (old[k].second != old[k + 1].second * old[k + 1].first) return std::nullopt;
+    int64_t st = old[oj - 1].second;
+    for (size_t k = nj; k-- > ni;) {
+      nst[k] = st;
+      st *= ns[k];
+    }
+    oi = oj;
+    ni = nj;
+  }
+  for (; ni < nn; ni++) {
+    if (ns[ni] != 1) return std::nullopt;
+    nst[ni] = 0;
+  }
+  return Affine{a.offset, ns, nst};
+}
+
 template <typename T>
 class CuNArray;
 template <typename T>
@@ -582,6 +627,9 @@ class CuView {
   }
   // View#reverse! (view.cr:96-99).
   CuView reverse() const { return CuView(buf_, affine_reverse(aff_)); }
+  // View#reshape (view.cr:58-70): the same elements in lexicographic order
+  // under a new shape; a layout that strides cannot express is copied first.
+  CuView reshape(const std::vector<int64_t>& new_shape) const;
 
   // View#to_narr (view.cr:123-126): one gather into a new contiguous array.
   CuNArray<T> to_cu() const;
@@ -697,6 +745,114 @@ class CuNArray : public CuView<T> {
   CuNArray& map_inplace(F f);
   template <typename U, typename F>
   CuNArray& map_with_inplace(const CuView<U>& other, F f);
+  // NArray#map_with_index! (n_array.cr:631-637) and #map_with_coord!
+  // (mutable.cr:16-20, n_array.cr:641-650): the block also receives the
+  // element's lexicographic index, or its coordinates, as Int32 Syms computed
+  // on the device (index operands, never stored).
+  template <typename F>
+  CuNArray& map_with_index_inplace(F f);
+  template <typename F>
+  CuNArray& map_with_coord_inplace(F f);
+
+  // NArray#reshape (n_array.cr:429-437): the same buffer under a new shape.
+  CuNArray reshape(const std::vector<int64_t>& new_shape) const {
+    if (count(new_shape) != count(this->shape()))
+      throw ShapeError("Cannot create NArray: Given shape does not match number of elements in buffer.");
+    return CuNArray(this->buf_, new_shape);
+  }
+
+  // NArray.tile (n_array.cr:242-252): src repeated counts[i] times along axis
+  // i.  One strided copy: the output seen as [c0, s0, c1, s1, ...] receives
+  // the source read with stride 0 along every c axis (leading axes walked on
+  // the host where that view would pass the device's rank limit).
+  static CuNArray tile(const CuView<T>& src, const std::vector<int64_t>& counts) {
+    const std::vector<int64_t>& ss = src.shape();
+    const size_t R = ss.size();
+    if (counts.size() < R)
+      throw IndexError("tile: " + std::to_string(counts.size()) + " counts for a " + std::to_string(R) +
+                       "-dimensional source");
+    std::vector<int64_t> shape(R);
+    for (size_t i = 0; i < R; i++) {
+      if (counts[i] < 0) throw ArgumentError("tile: negative count");
+      shape[i] = ss[i] * counts[i];
+    }
+    CuNArray out(shape);
+    if (shape_to_size(shape) == 0) return out;
+    const std::vector<int64_t> ost = row_major(shape);
+    const size_t lead = 2 * R > (size_t)PHCU_MAX_RANK ? 2 * R - (size_t)PHCU_MAX_RANK : 0;
+    int64_t nprefix = 1;
+    for (size_t i = 0; i < lead; i++) nprefix *= counts[i];
+    for (int64_t pfx = 0; pfx < nprefix; pfx++) {
+      Affine d{0, {}, {}}, s{src.layout().offset, {}, {}};
+      int64_t rest = pfx;
+      for (size_t i = lead; i-- > 0;) {  // this prefix's copy index along each leading axis
+        const int64_t ci = rest % counts[i];
+        rest /= counts[i];
+        d.offset += ci * ss[i] * ost[i];
+      }
+      for (size_t i = 0; i < R; i++) {
+        if (i < lead) {
+          d.shape.push_back(ss[i]);
+          d.stride.push_back(ost[i]);
+          s.shape.push_back(ss[i]);
+          s.stride.push_back(src.layout().stride[i]);
+        } else {
+          d.shape.insert(d.shape.end(), {counts[i], ss[i]});
+          d.stride.insert(d.stride.end(), {ss[i] * ost[i], ost[i]});
+          s.shape.insert(s.shape.end(), {counts[i], ss[i]});
+          s.stride.insert(s.stride.end(), {0, src.layout().stride[i]});
+        }
+      }
+      const phcu_view_t dv = make_view(out.buf_->ptr, DType<T>::id, d);
+      const phcu_view_t sv = make_view(src.buffer()->ptr, DType<T>::id, s);
+      check(phcu_copy(&dv, &sv), "phcu_copy");
+    }
+    return out;
+  }
+
+  // NArray.concatenate (n_array.cr:719-749): one strided copy of each operand
+  // into its slab of the output along `axis`.
+  static CuNArray concatenate(const std::vector<CuView<T>>& parts, int axis = 0) {
+    if (parts.empty()) throw ArgumentError("concatenate: no arrays");
+    const std::vector<int64_t>& first = parts[0].shape();
+    const int rank = (int)first.size();
+    const int ax = axis < 0 ? axis + rank : axis;
+    if (ax < 0 || ax >= rank)
+      throw IndexError("axis " + std::to_string(axis) + " is not present in a " + std::to_string(rank) +
+                       "-dimensional MultiIndexable");
+    std::vector<int64_t> shape = first;
+    shape[(size_t)ax] = 0;
+    for (const CuView<T>& p : parts) {
+      bool ok = (int)p.dimensions() == rank;
+      for (int i = 0; ok && i < rank; i++) ok = i == ax || p.shape()[(size_t)i] == first[(size_t)i];
+      if (!ok)
+        throw DimensionError("Cannot concatenate these arrays along axis " + std::to_string(axis) +
+                             ": shapes do not match");
+      shape[(size_t)ax] += p.shape()[(size_t)ax];
+    }
+    CuNArray out(shape);
+    const std::vector<int64_t> ost = row_major(shape);
+    int64_t pos = 0;
+    for (const CuView<T>& p : parts) {
+      const int64_t k = p.shape()[(size_t)ax];
+      if (k > 0 && p.size() > 0) {
+        std::vector<int64_t> sub = shape;
+        sub[(size_t)ax] = k;
+        const phcu_view_t dv = make_view(out.buf_->ptr, DType<T>::id, Affine{pos * ost[(size_t)ax], sub, ost});
+        const phcu_view_t sv = p.desc();
+        check(phcu_copy(&dv, &sv), "phcu_copy");
+      }
+      pos += k;
+    }
+    return out;
+  }
+
+  // NArray#push / #<< (n_array.cr:682-712): appends along axis 0; the array
+  // takes the concatenation's buffer.
+  CuNArray& push(const CuView<T>& other) {
+    *this = concatenate({*this, other}, 0);
+    return *this;
+  }
 
  private:
   static int64_t count(const std::vector<int64_t>& shape) {
@@ -760,7 +916,26 @@ class CuNArray : public CuView<T> {
   }
   template <typename R>
   void write_self(const CuProcView<R>& pv);
+  CuNArray(std::shared_ptr<Buffer> buf, const std::vector<int64_t>& shape)
+      : CuView<T>(std::move(buf), Affine{0, shape, row_major(shape)}) {}
 };
+
+template <typename T>
+CuView<T> CuView<T>::reshape(const std::vector<int64_t>& new_shape) const {
+  if (shape_to_size(new_shape) != size()) {
+    auto text = [](const std::vector<int64_t>& v) {
+      std::string t;
+      for (size_t i = 0; i < v.size(); i++) t += (i ? "x" : "") + std::to_string(v[i]);
+      return t;
+    };
+    throw ShapeError("Cannot change shape from " + text(aff_.shape) + " (" + std::to_string(size()) +
+                     " elements) to " + text(new_shape) + " (" + std::to_string(shape_to_size(new_shape)) +
+                     " elements) because reshape cannot add or remove elements.");
+  }
+  if (const std::optional<Affine> r = affine_reshape(aff_, new_shape)) return CuView(buf_, *r);
+  const CuNArray<T> m = to_cu();  // not expressible with strides: read now into a contiguous copy
+  return CuView(m.buffer(), Affine{0, new_shape, row_major(new_shape)});
+}
 
 template <typename T>
 CuNArray<T> CuView<T>::to_cu() const {
@@ -1154,7 +1329,7 @@ struct Leaf {
   std::shared_ptr<Buffer> buf;
   Affine aff;
   int32_t dtype = 0;
-  phcu_view_t desc() const { return make_view(buf->ptr, dtype, aff); }
+  phcu_view_t desc() const { return make_view(buf ? buf->ptr : nullptr, dtype, aff); }
   bool same(const Leaf& o) const {
     return buf.get() == o.buf.get() && dtype == o.dtype && aff.offset == o.aff.offset && aff.shape == o.aff.shape &&
            aff.stride == o.aff.stride;
@@ -1413,6 +1588,38 @@ CuNArray<T>& CuNArray<T>::map_with_inplace(const CuView<U>& other, F f) {
   write_self(CuProcView<R>({detail::Leaf{this->buf_, this->aff_, DType<T>::id},
                             detail::Leaf{other.buffer(), other.layout(), DType<U>::id}},
                            r.e, this->shape()));
+  return *this;
+}
+
+template <typename T>
+template <typename F>
+CuNArray<T>& CuNArray<T>::map_with_index_inplace(F f) {
+  auto r = f(Sym<T>::input(0), Sym<int32_t>::input(1));
+  static_assert(detail::IsSym<decltype(r)>::value, "a map_with_index! block returns a Sym");
+  using R = typename decltype(r)::value_type;
+  const std::vector<int64_t>& sh = this->shape();
+  write_self(CuProcView<R>({detail::Leaf{this->buf_, this->aff_, DType<T>::id},
+                            detail::Leaf{nullptr, Affine{0, sh, row_major(sh)}, PHCU_INDEX}},
+                           r.e, sh));
+  return *this;
+}
+
+template <typename T>
+template <typename F>
+CuNArray<T>& CuNArray<T>::map_with_coord_inplace(F f) {
+  const std::vector<int64_t>& sh = this->shape();
+  std::vector<detail::Leaf> leaves = {detail::Leaf{this->buf_, this->aff_, DType<T>::id}};
+  std::vector<Sym<int32_t>> coord;
+  for (size_t d = 0; d < sh.size(); d++) {  // coordinate d: stride 1 on axis d, 0 elsewhere
+    std::vector<int64_t> st(sh.size(), 0);
+    st[d] = 1;
+    leaves.push_back(detail::Leaf{nullptr, Affine{0, sh, st}, PHCU_INDEX});
+    coord.push_back(Sym<int32_t>::input((int32_t)(d + 1)));
+  }
+  auto r = f(Sym<T>::input(0), coord);
+  static_assert(detail::IsSym<decltype(r)>::value, "a map_with_coord! block returns a Sym");
+  using R = typename decltype(r)::value_type;
+  write_self(CuProcView<R>(std::move(leaves), r.e, sh));
   return *this;
 }
 

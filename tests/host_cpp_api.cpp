@@ -2,7 +2,8 @@
 // (ph-core_gb300/host/phase.hpp) as a caller uses it: views,
 // eager operators with Crystal's result types, fused CuProcView chains,
 // reductions, chunk reads and writes, element access, slices, comparisons,
-// masked writes, equality, in-place maps, region operations.  The static
+// masked writes, equality, in-place maps, reshape, tile, concatenate, push,
+// region operations.  The static
 // assertions pin the result types; tests/test_host_cpp_programs.py compiles
 // this file with warnings as errors.  Nothing here runs.
 #include <type_traits>
@@ -75,6 +76,15 @@ void api(const std::vector<float>& host_f, const std::vector<int32_t>& host_i) {
   CuNArray<float>& self = a.map_inplace([](auto e) { return e * 3 + 1; });
   ai.map_with_inplace(bi.view({}), [](auto u, auto v) { return u - v * 2; });
   a.map_with_inplace(ai.view({}), [](auto u, auto v) { return u * v; });  // Float32 * Int32 stays Float32
+  a.map_with_index_inplace([](auto e, auto k) { return e + k; });
+  ai.map_with_coord_inplace([](auto e, const auto& cd) { return e * cd[0] - cd[2]; });
+
+  // reshape, tile, concatenate, push
+  CuView<float> rv = p.reshape({256, 512 * 512});
+  CuNArray<float> ra = a.reshape({512 * 512, 256});
+  CuNArray<float> tl = CuNArray<float>::tile(a.get_chunk({rng(0, 1)}), {2, 1, 3});
+  CuNArray<float> cc = CuNArray<float>::concatenate({a.view({}), b.view({})}, 2);
+  ai.push(bi.view({}));
 
   // region operations
   IndexRegion reg = IndexRegion::absolute({rng(3, 20, 4), rng(7, std::nullopt, -2)});
@@ -85,5 +95,5 @@ void api(const std::vector<float>& host_f, const std::vector<int32_t>& host_i) {
   std::vector<int64_t> abs = reg.local_to_absolute({1, 2});
   reg.trim({10, 4});
   (void)i, (void)q, (void)w, (void)out, (void)s1, (void)am, (void)corner, (void)total, (void)where;
-  (void)fits, (void)has, (void)abs, (void)r, (void)e0, (void)sl, (void)mh, (void)eqs, (void)self;
+  (void)fits, (void)has, (void)abs, (void)r, (void)e0, (void)sl, (void)mh, (void)eqs, (void)self, (void)rv, (void)ra, (void)tl, (void)cc;
 }

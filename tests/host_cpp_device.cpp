@@ -4,7 +4,8 @@
 // per result or raised exception; tests/test_gpu_host_cpp.py compares them
 // with the oracle.  With argv[2] = "proc" it runs the fused expressions
 // (CuProcView) instead of the eager operators; with "more" element access,
-// slices, comparisons, masked writes, equality and in-place maps.
+// slices, comparisons, masked writes, equality, in-place maps, reshape, tile,
+// concatenate and push.
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -162,6 +163,27 @@ static void run_more(const std::string& tag) {
   std::cout << "equals " << tag << " other " << equals(A, B) << "\n";
   std::cout << "equals " << tag << " reversed " << equals(A.view(rev), A.view(rev).to_cu()) << "\n";
   std::cout << "equals " << tag << " shape " << equals(A.view({}), A.permute({2, 0, 1})) << "\n";
+  // reshape: a permuted view (copied first), an affine one, the array itself
+  save(tag + "_reshape_perm", A.permute({2, 0, 1}).reshape({10, 192}).to_vector());
+  save(tag + "_reshape_rows", A.view({rng(2, 9)}).reshape({8, 120}).to_vector());
+  save(tag + "_reshape_rev", A.view(rev).reshape({16, 120}).to_vector());
+  save(tag + "_reshape_array", A.reshape({120, 16}).to_vector());
+  expect_raise(tag + "_reshape_size", [&] { return A.view({}).reshape({7, 7}); });
+  // tile, concatenate, push
+  const CuNArray<T> S = A.get_chunk({rng(0, 3), rng(0, 4), rng(0, 5)});
+  save(tag + "_tile", CuNArray<T>::tile(S.view(rev), {2, 3, 1}).to_vector());
+  save(tag + "_concat", CuNArray<T>::concatenate({A.view(rev), B.view({})}, 1).to_vector());
+  expect_raise(tag + "_concat_dim", [&] { return CuNArray<T>::concatenate({A.view({}), A.permute({2, 0, 1})}, 0); });
+  CuNArray<T> P = A.clone();
+  P.push(B.view({}));
+  save(tag + "_push", P.to_vector());
+  // in-place maps with the element's index and coordinates
+  CuNArray<T> I = A.clone();
+  I.map_with_index_inplace([](auto e, auto i) { return e + i; });
+  save(tag + "_map_with_index", I.to_vector());
+  CuNArray<T> K = A.clone();
+  K.map_with_coord_inplace([](auto e, const auto& c) { return e * c[0] - c[2]; });
+  save(tag + "_map_with_coord", K.to_vector());
 }
 
 static void run_proc_mixed() {

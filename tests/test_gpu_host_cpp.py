@@ -121,6 +121,38 @@ def test_element_access_slices_masks_equality_and_inplace_maps(run_more, ora, cu
 
 
 @pytest.mark.parametrize("tag", ["f32", "i32"])
+def test_reshape_tile_concatenate_push_and_index_maps(run_more, ora, cu, tag):
+    """View#reshape (affine, or copied first where strides cannot express the
+    new shape), NArray#reshape, NArray.tile, NArray.concatenate, #push and the
+    in-place maps with the element's index and coordinates of the C++ mirror,
+    against the oracle (bit-exact)."""
+    arrays, lines, load = run_more
+    a, b = arrays[tag]
+    dt = a.dtype
+    rev = lambda x: np.ascontiguousarray(x[:, ::-1, :])  # noqa: E731
+    assert np.array_equal(load(tag + "_reshape_perm", dt), np.transpose(a, (2, 0, 1)).reshape(-1))
+    assert np.array_equal(load(tag + "_reshape_rows", dt), a[2:10].reshape(-1))
+    assert np.array_equal(load(tag + "_reshape_rev", dt), rev(a).reshape(-1))
+    assert np.array_equal(load(tag + "_reshape_array", dt), a.reshape(-1))
+    assert "raised %s_reshape_size ShapeError" % tag in lines
+    s = ora.narray_fetch_chunk(a, [cu.R(0, 3), cu.R(0, 4), cu.R(0, 5)])
+    assert s.shape == (4, 5, 6)
+    assert np.array_equal(load(tag + "_tile", dt), ora.tile(rev(s), [2, 3, 1]).reshape(-1))
+    assert np.array_equal(load(tag + "_concat", dt), ora.concatenate([rev(a), b], 1).reshape(-1))
+    assert "raised %s_concat_dim DimensionError" % tag in lines
+    assert np.array_equal(load(tag + "_push", dt), ora.concatenate([a, b], 0).reshape(-1))
+    index = np.arange(a.size, dtype=np.int32).reshape(a.shape)
+    mi, _ = ora.map_binary(ora.OP_ADD, a, index)
+    assert mi.dtype == dt
+    assert np.array_equal(load(tag + "_map_with_index", dt), mi.reshape(-1))
+    c0 = np.broadcast_to(np.arange(a.shape[0], dtype=np.int32)[:, None, None], a.shape).copy()
+    c2 = np.broadcast_to(np.arange(a.shape[2], dtype=np.int32)[None, None, :], a.shape).copy()
+    mc, _ = ora.map_binary(ora.OP_MUL, a, c0)
+    mc, _ = ora.map_binary(ora.OP_SUB, mc, c2)
+    assert np.array_equal(load(tag + "_map_with_coord", dt), mc.reshape(-1))
+
+
+@pytest.mark.parametrize("tag", ["f32", "i32"])
 def test_views_operators_and_chunks(run, ora, cu, tag):
     arrays, lines, load = run
     a, b = arrays[tag]
