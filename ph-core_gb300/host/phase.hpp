@@ -11,6 +11,13 @@
 // descriptor (offset, shape, signed strides) over an array's device buffer;
 // nothing is copied until an operation materialises it.  Every bulk
 // operation is one call into the library; there is no CPU path.
+//
+// Surface: CuNArray<T> (arrays), CuView<T> (region / permute / reverse /
+// reshape views), CuProcView<T> (fused expressions: one device program per
+// materialisation), the infix operators with Crystal's result types and the
+// comparisons (Bool arrays), reductions, chunk and element reads and writes,
+// slices, masked writes, equals?, the in-place maps (map!, map_with!,
+// map_with_index!, map_with_coord!), tile, concatenate and push.
 #pragma once
 
 #include <algorithm>
