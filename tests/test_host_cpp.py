@@ -2,7 +2,8 @@
 IndexRegion logic (canonicalisation, absolute regions, fits_in?, trim!,
 reverse!, translate!, includes?, local_to_absolute) against the reference's
 TestRanges and IndexRegion KATs, and against the Python mirror (itself pinned
-by those KATs) on 3,000 random regions and operations.  Host logic only:
+by those KATs) on 3,000 random regions and operations; its affine reshape of
+views against the Python mirror's on 4,000 random layouts.  Host logic only:
 compiled with g++, no GPU."""
 import os
 import random
@@ -179,3 +180,83 @@ def test_random_regions_and_operations_match_the_python_mirror(exe):
     out = _run(exe, cases)
     for (bound, lits, op), o in zip(cases, out):
         assert o == " ".join(_python(bound, lits, op).split()), (bound, lits, op, o)
+
+
+def test_affine_reshape_matches_python_mirror(tmp_path):
+    """View#reshape as strides (the C++ mirror's affine_reshape) gives the
+    Python mirror's answer on random layouts: row-major arrays seen through
+    random regions with steps, reversals and permutations, reshaped to random
+    factorisations of their element count (some expressible with strides,
+    some not).  Where both give strides, the lexicographic element addresses
+    of the new view equal those of the old one."""
+    import itertools
+
+    import numpy as np
+
+    from phase_cu import narray
+
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not available")
+    exe = str(tmp_path / "host_cpp_reshape")
+    cmd = [gxx, "-std=c++17", "-O1", "-Wall", "-o", exe, os.path.join(ROOT, "tests", "host_cpp_reshape.cpp"),
+           "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "ph-core_gb300", "host")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    rng = random.Random(11)
+
+    def factorisation(n, rank):
+        dims = []
+        for _ in range(rank - 1):
+            divs = [d for d in range(1, n + 1) if n % d == 0]
+            d = rng.choice(divs)
+            dims.append(d)
+            n //= d
+        dims.append(n)
+        rng.shuffle(dims)
+        return dims
+
+    def addresses(off, shape, stride):
+        return [off + sum(c * s for c, s in zip(idx, stride)) for idx in itertools.product(*map(range, shape))]
+
+    cases = []
+    for _ in range(4000):
+        base = [rng.randint(1, 6) for _ in range(rng.randint(1, 4))]
+        st = narray._row_major(base)
+        off, shape, stride = 0, [], []
+        for n, s in zip(base, st):  # a region with a step, maybe reversed
+            step = rng.choice([1, 1, 1, 2, 3])
+            k = (n - 1) // step + 1
+            if rng.random() < 0.3:
+                off += (n - 1) * s
+                shape.append(k)
+                stride.append(-step * s)
+            else:
+                shape.append(k)
+                stride.append(step * s)
+        perm = list(range(len(shape)))
+        if rng.random() < 0.4:
+            rng.shuffle(perm)
+        shape = [shape[p] for p in perm]
+        stride = [stride[p] for p in perm]
+        n = int(np.prod(shape))
+        new = factorisation(n, rng.randint(1, 4))
+        cases.append((off, shape, stride, new))
+    lines = []
+    for off, shape, stride, new in cases:
+        lines.append(" ".join(map(str, [off, len(shape)] + shape + stride + [len(new)] + new)))
+    p = subprocess.run([exe], input="\n".join(lines) + "\n", capture_output=True, text=True, timeout=120)
+    assert p.returncode == 0, p.stderr[-2000:]
+    out = p.stdout.splitlines()
+    assert len(out) == len(cases)
+    affine = 0
+    for (off, shape, stride, new), got in zip(cases, out):
+        exp = narray._affine_reshape(off, shape, stride, new)
+        if exp is None:
+            assert got == "NONE", (off, shape, stride, new, got)
+            continue
+        eoff, _, est = exp
+        assert got == "OK " + " ".join(str(int(v)) for v in [eoff] + list(est)), (off, shape, stride, new, got)
+        assert addresses(eoff, new, est) == addresses(off, shape, stride)
+        affine += 1
+    assert 1000 < affine < len(cases)  # both outcomes are exercised
