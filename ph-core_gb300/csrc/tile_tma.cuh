@@ -5,7 +5,8 @@
 // described once per launch by a tensor map over the plan's axes
 // [R, W, batch...].  One thread per block issues cp.async.bulk.tensor copies
 // of two 32x64 boxes (128-byte rows, 128B swizzle) per input and tile into a
-// two-stage ring; an mbarrier per stage counts the bytes in.  The other
+// ring of stages (one to four by kernel kind, tma_stages); an mbarrier per
+// stage counts the bytes in.  The other
 // threads spend no instructions on staging: each reads 16-byte chunks of four
 // consecutive R elements of one W row (the swizzle puts the eight rows of a
 // quarter-warp in eight different bank groups, so the transposed reads are
