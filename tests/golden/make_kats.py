@@ -138,6 +138,17 @@ def kats():
         "reshape": {"src_shape": [3, 4], "new_shape": [6, 2], "coord": [2, 1], "expected": [1, 1]},
         "reverse": {"shape": [5, 3], "coord": [1, 2], "expected": [3, 0]},
     }
+    # spec/multi_indexable/elem_iterator_spec.cr:7-67 and elem_coord_iterator_spec.cr:7-59:
+    # NArray[[1, 2, 3], [4, 5, 6], [7, 8, 9]] iterated in lexicographic and
+    # colexicographic order (elements, and elements with coordinates); reverse_each
+    # yields each sequence backwards
+    k["elem_iterators"] = {
+        "narr": [[1, 2, 3], [4, 5, 6], [7, 8, 9]],
+        "lex": [1, 2, 3, 4, 5, 6, 7, 8, 9],
+        "lex_coords": [[0, 0], [0, 1], [0, 2], [1, 0], [1, 1], [1, 2], [2, 0], [2, 1], [2, 2]],
+        "colex": [1, 4, 7, 2, 5, 8, 3, 6, 9],
+        "colex_coords": [[0, 0], [1, 0], [2, 0], [0, 1], [1, 1], [2, 1], [0, 2], [1, 2], [2, 2]],
+    }
     # spec/multi_writable_spec.cr:14-65 (Int32 payload; the spec's buffer mixes types)
     k["multi_writable"] = {"shape": [3, 4], "buffer": list(range(1, 13)), "literal": [Rg(1, None), Rg(1, None)],
                            "scalar": 10, "scalar_indices": [5, 6, 7, 9, 10, 11],

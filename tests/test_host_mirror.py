@@ -282,6 +282,37 @@ def test_int32_division_to_float64_is_correctly_rounded():
             assert _int32_div_f64_bits(x, y, 1) == exp and _int32_div_f64_bits(x, y, -1) == exp, (x, y)
 
 
+def test_index_operands_follow_the_reference_iteration_order(kats):
+    """The host mirror's view descriptors against the element-iterator KATs
+    (spec/multi_indexable/elem_iterator_spec.cr, elem_coord_iterator_spec.cr),
+    evaluated on the host: the coordinate operands of map_with_coord (index
+    views, stride 1 on their axis) give the lexicographic coordinates, and the
+    same operands and the array itself seen through permute(1, 0) give the
+    colexicographic coordinates and elements; a reversal of every axis
+    (reverse_each) the lexicographic elements backwards."""
+    import itertools
+
+    from phase_cu import narray
+
+    k = kats["elem_iterators"]
+    narr = np.array(k["narr"], dtype=np.int32)
+    shape = list(narr.shape)
+
+    def walk(off, shp, st):
+        return [off + sum(c * s for c, s in zip(ix, st)) for ix in itertools.product(*map(range, shp))]
+
+    axes = [narray.CuIndexView.axis(shape, d) for d in range(2)]
+    lex = [list(c) for c in zip(*(walk(*a._desc()[1:]) for a in axes))]
+    assert lex == k["lex_coords"]
+    colex = [list(c) for c in zip(*(walk(*a.permute(1, 0)._desc()[1:]) for a in axes))]
+    assert colex == k["colex_coords"]
+    flat = narr.reshape(-1)
+    off, shp, st = narray._affine_permute(0, shape, narray._row_major(shape), [1, 0])
+    assert [int(flat[i]) for i in walk(off, shp, st)] == k["colex"]
+    off, shp, st = narray._affine_reverse(0, shape, narray._row_major(shape))
+    assert [int(flat[i]) for i in walk(off, shp, st)] == k["lex"][::-1]
+
+
 def _header_functions():
     with open(os.path.join(ROOT, "include", "phcuda.h")) as f:
         text = f.read()

@@ -187,6 +187,31 @@ def test_transforms(ora, kats):
     assert ora.xf_apply(ora.TF_REVERSE, t["reverse"]["coord"], shape=t["reverse"]["shape"]) == t["reverse"]["expected"]
 
 
+def test_elem_iterators(ora, kats):
+    """The lexicographic and colexicographic iteration orders of the reference's
+    element iterators (spec/multi_indexable/elem_iterator_spec.cr,
+    elem_coord_iterator_spec.cr): every bulk operation writes its output in
+    lexicographic order, so the gather of the array is the lexicographic
+    sequence, the gather of its transpose the colexicographic one, and the
+    gather of its reversal the reversed sequence (reverse_each); the
+    coordinate operands (map_with_coord) give the coordinates in the same
+    orders."""
+    k = kats["elem_iterators"]
+    narr = np.array(k["narr"], dtype=np.int32)
+    from phase_cu.region import R
+
+    assert ora.gather(ora.ViewOperand(narr)).reshape(-1).tolist() == k["lex"]
+    assert ora.gather(ora.ViewOperand(narr, [("permute", [1, 0])])).reshape(-1).tolist() == k["colex"]
+    rev = [("region", [R(None, None, -1), R(None, None, -1)])]
+    assert ora.gather(ora.ViewOperand(narr, rev)).reshape(-1).tolist() == k["lex"][::-1]
+    c0, c1 = ora.coords(narr.shape)
+    lex = [[int(a), int(b)] for a, b in zip(c0.reshape(-1), c1.reshape(-1))]
+    assert lex == k["lex_coords"]
+    t0 = ora.gather(ora.ViewOperand(c0, [("permute", [1, 0])])).reshape(-1)
+    t1 = ora.gather(ora.ViewOperand(c1, [("permute", [1, 0])])).reshape(-1)
+    assert [[int(a), int(b)] for a, b in zip(t0, t1)] == k["colex_coords"]
+
+
 def test_multi_writable(ora, kats):
     k = kats["multi_writable"]
     buf = np.array(k["buffer"], dtype=np.int32).reshape(k["shape"])
