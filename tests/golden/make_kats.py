@@ -121,6 +121,15 @@ def kats():
         "mask_scalar_6": [[6, 1, 6], [3, 6, 5]],
         "mask_src_plus_10": [[10, 1, 12], [3, 14, 5]],
     }
+    # spec/n_array_spec.cr:444-518: #map, #map_with_coord, #map_with_index and their in-place forms
+    # on stock_narr (map { x ** 2 }; map_with_coord { 10 * c[0] + c[1] + el };
+    # (stock_narr * 2).map_with_index { idx + el } == stock_narr * 3)
+    k["narray_maps"] = {
+        "stock": stock,
+        "map_pow_2": [[0, 1, 4], [9, 16, 25]],
+        "map_with_coord": [[0, 2, 4], [13, 15, 17]],
+        "map_with_index_of_times_2": [[0, 3, 6], [9, 12, 15]],
+    }
     k["serialization"] = {  # spec/n_array_spec.cr:520-557
         "stock_json": '{"shape":[2,3],"elements":[0,1,2,3,4,5]}',
         "empty_json": '{"shape":[0],"elements":[]}',

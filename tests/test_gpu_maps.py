@@ -23,6 +23,28 @@ def _i32(shape, seed):
     return np.random.default_rng(seed).integers(-1000, 1000, shape).astype(np.int32)
 
 
+def test_reference_map_kats_on_device(cu, kats):
+    """NArray#map, #map_with_coord, #map_with_index and the in-place forms
+    map!, map_with_coord!, map_with_index! on the spec's stock array
+    (spec/n_array_spec.cr:444-518), on the device."""
+    k = kats["narray_maps"]
+    stock = np.array(k["stock"], dtype=np.int32)
+    S = cu.CuNArray.from_numpy(stock)
+    assert S.map(lambda x: x ** 2).to_narr().tolist() == k["map_pow_2"]
+    assert S.map_with_coord(lambda el, c: 10 * c[0] + c[1] + el).to_narr().tolist() == k["map_with_coord"]
+    T = cu.CuNArray.from_numpy(stock * 2)
+    assert T.map_with_index(lambda el, idx: idx + el).to_narr().tolist() == k["map_with_index_of_times_2"]
+    M = S.clone()
+    assert M.map_inplace(lambda x: x ** 2) is M
+    assert M.to_narr().tolist() == k["map_pow_2"]
+    C = S.clone()
+    assert C.map_with_coord_inplace(lambda el, c: 10 * c[0] + c[1] + el) is C
+    assert C.to_narr().tolist() == k["map_with_coord"]
+    I = cu.CuNArray.from_numpy(stock * 2)  # noqa: E741
+    assert I.map_with_index_inplace(lambda el, idx: idx + el) is I
+    assert I.to_narr().tolist() == k["map_with_index_of_times_2"]
+
+
 def test_map_with_index(cu, ora):
     shape = [6, 33, 17]
     a = _f32(shape, 0)

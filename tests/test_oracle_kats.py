@@ -212,6 +212,24 @@ def test_elem_iterators(ora, kats):
     assert [[int(a), int(b)] for a, b in zip(t0, t1)] == k["colex_coords"]
 
 
+def test_narray_maps(ora, kats):
+    """NArray#map, #map_with_coord and #map_with_index (spec/n_array_spec.cr:
+    444-518) on the oracle: the block evaluated per element with the
+    coordinates / lexicographic index operands, Crystal Int32 arithmetic."""
+    k = kats["narray_maps"]
+    stock = np.array(k["stock"], dtype=np.int32)
+    sq, _ = ora.map_binary_scalar(ora.OP_POW, stock, 2, ora.I32)
+    assert sq.tolist() == k["map_pow_2"]
+    c0, c1 = ora.coords(stock.shape)
+    t, _ = ora.map_binary_scalar(ora.OP_MUL, c0, 10, ora.I32, scalar_left=True)
+    t, _ = ora.map_binary(ora.OP_ADD, t, c1)
+    t, _ = ora.map_binary(ora.OP_ADD, t, stock)
+    assert t.tolist() == k["map_with_coord"]
+    twice, _ = ora.map_binary_scalar(ora.OP_MUL, stock, 2, ora.I32)
+    t, _ = ora.map_binary(ora.OP_ADD, ora.lex_index(stock.shape), twice)
+    assert t.tolist() == k["map_with_index_of_times_2"]
+
+
 def test_multi_writable(ora, kats):
     k = kats["multi_writable"]
     buf = np.array(k["buffer"], dtype=np.int32).reshape(k["shape"])
